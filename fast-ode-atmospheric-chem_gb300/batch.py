@@ -1,0 +1,91 @@
+"""Batched, device-resident integration of many groups of one mechanism.
+
+``Batch`` keeps the state of C cells on the GPU in the species-major layout
+(n, C), cells fastest, with one controller memory, one counter row and one
+status per group, and integrates every group over an interval with a single
+``fo_solve`` launch. It is the device-side form of the reference's scenario
+loop (fastode/ts1.py:196-222): per group a Memory carried across intervals,
+per interval fresh rate constants.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .counts import COUNT_FIELDS, Counts
+from .plan import plan_for
+from .solvers import Algorithm
+
+
+def group_offsets(n_cells: int, group_size: int) -> np.ndarray:
+    """Contiguous groups of `group_size` cells; the last one may be short
+    (fastode/ts1.py:196-197)."""
+    starts = list(range(0, n_cells, group_size)) + [n_cells]
+    return np.array(starts, dtype=np.int32)
+
+
+class Batch:
+    def __init__(self, mech, Y0, group_size: int = 32, algorithm: Algorithm = None, mass=None,
+                 offsets=None, slots: int = 0, trace_cap: int = 0, stream=None):
+        import torch
+        self.torch = torch
+        self.alg = algorithm if algorithm is not None else Algorithm()
+        self.plan = plan_for(mech, mass, self.alg.ordering)
+        dev = torch.device("cuda", self.plan.device)
+        self.dev = dev
+        Y0 = Y0 if isinstance(Y0, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(Y0, dtype=np.float64))
+        self.C, n = Y0.shape
+        if n != self.plan.n:
+            raise ValueError(f"Y0 has {n} species, the mechanism {self.plan.n}")
+        offs = group_offsets(self.C, group_size) if offsets is None else np.asarray(offsets, dtype=np.int32)
+        self.offsets_host = offs
+        self.ngroups = len(offs) - 1
+        self.max_cells = int(np.max(np.diff(offs)))
+        self.offsets = torch.from_numpy(offs).to(dev)
+        self.Y = Y0.to(dev, dtype=torch.float64).t().contiguous()          # (n, C)
+        self.memory = torch.zeros((self.ngroups, 3), dtype=torch.float64, device=dev)
+        self.counts = torch.zeros((self.ngroups, len(COUNT_FIELDS)), dtype=torch.int64, device=dev)
+        self.status = torch.zeros(self.ngroups, dtype=torch.int32, device=dev)
+        self.slots = int(slots)
+        grid = self.ngroups if self.slots <= 0 else min(self.slots, self.ngroups)
+        self.ws = torch.empty(self.plan.workspace_bytes(grid, self.max_cells), dtype=torch.uint8, device=dev)
+        self.trace_cap = int(trace_cap)
+        if self.trace_cap > 0:
+            self.trace = torch.zeros((self.ngroups, self.trace_cap, 4), dtype=torch.float64, device=dev)
+            self.trace_len = torch.zeros(self.ngroups, dtype=torch.int32, device=dev)
+        self.opts = self.alg.options()
+        self.stream = stream
+
+    def _stream(self):
+        s = self.stream if self.stream is not None else self.torch.cuda.current_stream(self.dev)
+        return s
+
+    def step(self, k, dt: float, atol, rtol: float) -> None:
+        """Integrate every group over one interval of length dt, asynchronously
+        on the batch's stream. k: device tensor (R, C), cells fastest; atol:
+        device tensor (n,)."""
+        s = self._stream()
+        rc = _abi.lib().fo_solve(
+            self.plan.handle, C.byref(self.opts), self.ngroups, self.offsets.data_ptr(), self.max_cells,
+            self.Y.data_ptr(), 1, self.C, k.data_ptr(), 1, self.C,
+            atol.data_ptr(), float(rtol), float(dt),
+            self.memory.data_ptr(), self.counts.data_ptr(), self.status.data_ptr(),
+            self.ws.data_ptr(), self.ws.numel(), self.slots,
+            self.trace.data_ptr() if self.trace_cap else None, self.trace_cap,
+            self.trace_len.data_ptr() if self.trace_cap else None, C.c_void_p(s.cuda_stream))
+        _abi.check(rc, "fo_solve")
+
+    def state(self) -> np.ndarray:
+        """The cells' state as (C, n) on the host."""
+        return self.Y.t().contiguous().cpu().numpy()
+
+    def total_counts(self) -> Counts:
+        c = Counts()
+        for row in self.counts.cpu().numpy():
+            c.add_row(row)
+        return c
+
+    def statuses(self) -> list:
+        return [_abi.STATUS_STRINGS[int(s)] for s in self.status.cpu().numpy()]

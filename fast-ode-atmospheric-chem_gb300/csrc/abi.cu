@@ -1,0 +1,345 @@
+// The C-ABI: plans, workspace sizing and launches. Every entry point returns
+// an FO_* code and never aborts; CUDA failures are reported with FO_E_CUDA
+// and the text of the error is kept for fo_last_error().
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+#include "fastode_gb300.h"
+#include "symbolic.h"
+
+namespace fo {
+cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream);
+cudaError_t launch_eval(const SolveParams& p, int C, int want_jac, double* out, cudaStream_t stream);
+}  // namespace fo
+
+struct fo_plan {
+  fo::HostTables host;
+  fo::DevTables dev;
+  void* blob = nullptr;  // device copy of every table
+  int device = -1;
+};
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+int fail(int code, const std::string& what) {
+  g_last_error = what;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return FO_E_CUDA;
+}
+
+const fo::DevTableau kTableaus[2] = {
+    // ROS3 (fastode/tableaus.py:70-80)
+    {0.43586652150845899941601945119356,
+     3,
+     {{0, 0, 0, 0}, {1.0, 0, 0, 0}, {1.0, 0.0, 0, 0}, {0, 0, 0, 0}},
+     {{0, 0, 0, 0},
+      {-0.10156171083877702091975600115545e01, 0, 0, 0},
+      {0.40759956452537699824805835358067e01, 0.92076794298330791242156818474003e01, 0, 0},
+      {0, 0, 0, 0}},
+     {1.0, 0.61697947043828245592553615689730e01, -0.42772256543218573326238373806514, 0},
+     {0.5, -0.29079558716805469821718236208017e01, 0.22354069897811569627360909276199, 0},
+     {1, 1, 0, 0}},
+    // RODAS3 (fastode/tableaus.py:82-90)
+    {0.5,
+     4,
+     {{0, 0, 0, 0}, {0.0, 0, 0, 0}, {2.0, 0.0, 0, 0}, {2.0, 0.0, 1.0, 0}},
+     {{0, 0, 0, 0}, {4.0, 0, 0, 0}, {1.0, -1.0, 0, 0}, {1.0, -1.0, -8.0 / 3.0, 0}},
+     {2.0, 0.0, 1.0, 1.0},
+     {0.0, 0.0, 0.0, 1.0},
+     {1, 0, 1, 1}},
+};
+
+fo::ScratchLayout layout_of(const fo::HostTables& t) {
+  fo::ScratchLayout s;
+  int64_t o = 0;
+  s.lu = o; o += (int64_t)t.lu_col.size();
+  s.negj = o; o += (int64_t)t.j_col.size();
+  s.d = o; o += (int64_t)t.R * t.P;
+  s.r = o; o += t.R;
+  s.y = o; o += t.n;
+  s.ynew = o; o += t.n;
+  s.f0 = o; o += t.n;
+  s.ft = o; o += t.n;
+  s.yr = o; o += t.n;
+  s.k = o; o += 4LL * t.n;
+  s.items = o;
+  return s;
+}
+
+int lanes_for(int cells) { return ((cells + 31) / 32) * 32; }
+
+size_t smem_bytes(const fo::HostTables& t, int lanes) { return sizeof(double) * (32 + (size_t)t.n * lanes); }
+
+constexpr size_t kHeader = 256;  // queue counter at the start of the workspace
+constexpr int kMaxLanes = 256;
+
+template <typename T>
+size_t append(std::vector<char>& buf, const std::vector<T>& v) {
+  size_t off = (buf.size() + 255) & ~size_t(255);
+  buf.resize(off + v.size() * sizeof(T) + 1);
+  if (!v.empty()) std::memcpy(buf.data() + off, v.data(), v.size() * sizeof(T));
+  return off;
+}
+
+void fill_info(const fo::HostTables& t, fo_plan_info* info) {
+  std::memset(info, 0, sizeof(*info));
+  info->n = t.n;
+  info->R = t.R;
+  info->P = t.P;
+  info->nnz_jac = t.nnz;
+  info->ordering = t.ordering;
+  info->nnz_lu = (int32_t)t.lu_col.size();
+  info->nnz_l = t.nnz_l;
+  info->nnz_u = t.nnz_u;
+  info->lu_fma = t.lu_fma;
+  info->solve_fma = t.solve_fma;
+  info->jac_terms = (int32_t)t.jt_idx.size();
+  info->stoich_nnz = (int32_t)t.s_rxn.size();
+  info->scratch_doubles_per_cell = layout_of(t).items;
+  info->smem_doubles_per_cell = t.n;
+}
+
+fo::SolveParams base_params(const fo_plan* plan) {
+  fo::SolveParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.t = plan->dev;
+  p.sl = layout_of(plan->host);
+  return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fo_last_error(void) { return g_last_error.c_str(); }
+
+int fo_analyze(const fo_mechanism_desc* mech, int32_t ordering, fo_plan_info* info, int32_t* perm) {
+  if (!mech || !info) return fail(FO_E_INVALID, "null argument");
+  try {
+    fo::HostTables t;
+    std::string err = fo::build_tables(*mech, ordering, &t);
+    if (!err.empty()) return fail(FO_E_INVALID, err);
+    fill_info(t, info);
+    if (perm) std::memcpy(perm, t.perm.data(), sizeof(int32_t) * t.n);
+  } catch (const std::bad_alloc&) {
+    return fail(FO_E_ALLOC, "host allocation failed");
+  }
+  return FO_OK;
+}
+
+int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** out) {
+  if (!mech || !out) return fail(FO_E_INVALID, "null argument");
+  *out = nullptr;
+  fo_plan* plan = new (std::nothrow) fo_plan;
+  if (!plan) return fail(FO_E_ALLOC, "host allocation failed");
+  try {
+    std::string err = fo::build_tables(*mech, ordering, &plan->host);
+    if (!err.empty()) {
+      delete plan;
+      return fail(FO_E_INVALID, err);
+    }
+  } catch (const std::bad_alloc&) {
+    delete plan;
+    return fail(FO_E_ALLOC, "host allocation failed");
+  }
+  const fo::HostTables& t = plan->host;
+  std::vector<char> buf;
+  size_t o_perm = append(buf, t.perm), o_mass = append(buf, t.mass), o_react = append(buf, t.react),
+         o_sptr = append(buf, t.s_ptr), o_srxn = append(buf, t.s_rxn), o_sval = append(buf, t.s_val),
+         o_jrow = append(buf, t.j_row_ptr), o_jcol = append(buf, t.j_col), o_jsrc = append(buf, t.j_src),
+         o_jtp = append(buf, t.jt_ptr), o_jti = append(buf, t.jt_idx), o_jtv = append(buf, t.jt_val),
+         o_lur = append(buf, t.lu_row_ptr), o_lud = append(buf, t.lu_diag), o_luc = append(buf, t.lu_col);
+  cudaError_t e = cudaGetDevice(&plan->device);
+  if (e != cudaSuccess) {
+    delete plan;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  e = cudaMalloc(&plan->blob, buf.size());
+  if (e != cudaSuccess) {
+    delete plan;
+    return cuda_fail(e, "cudaMalloc(plan tables)");
+  }
+  e = cudaMemcpy(plan->blob, buf.data(), buf.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(plan->blob);
+    delete plan;
+    return cuda_fail(e, "cudaMemcpy(plan tables)");
+  }
+  char* b = static_cast<char*>(plan->blob);
+  fo::DevTables& d = plan->dev;
+  d.n = t.n;
+  d.R = t.R;
+  d.P = t.P;
+  d.nlu = (int)t.lu_col.size();
+  d.nnzj = (int)t.j_col.size();
+  d.perm = reinterpret_cast<const int32_t*>(b + o_perm);
+  d.mass = reinterpret_cast<const double*>(b + o_mass);
+  d.react = reinterpret_cast<const int32_t*>(b + o_react);
+  d.s_ptr = reinterpret_cast<const int32_t*>(b + o_sptr);
+  d.s_rxn = reinterpret_cast<const int32_t*>(b + o_srxn);
+  d.s_val = reinterpret_cast<const double*>(b + o_sval);
+  d.j_row_ptr = reinterpret_cast<const int32_t*>(b + o_jrow);
+  d.j_col = reinterpret_cast<const int32_t*>(b + o_jcol);
+  d.j_src = reinterpret_cast<const int32_t*>(b + o_jsrc);
+  d.jt_ptr = reinterpret_cast<const int32_t*>(b + o_jtp);
+  d.jt_idx = reinterpret_cast<const int32_t*>(b + o_jti);
+  d.jt_val = reinterpret_cast<const double*>(b + o_jtv);
+  d.lu_row_ptr = reinterpret_cast<const int32_t*>(b + o_lur);
+  d.lu_diag = reinterpret_cast<const int32_t*>(b + o_lud);
+  d.lu_col = reinterpret_cast<const int32_t*>(b + o_luc);
+  d.has_constraints = 0;
+  for (double m : t.mass)
+    if (m == 0.0) d.has_constraints = 1;
+  *out = plan;
+  return FO_OK;
+}
+
+int fo_plan_info_get(const fo_plan* plan, fo_plan_info* info) {
+  if (!plan || !info) return fail(FO_E_INVALID, "null argument");
+  fill_info(plan->host, info);
+  return FO_OK;
+}
+
+int fo_plan_destroy(fo_plan* plan) {
+  if (!plan) return FO_OK;
+  if (plan->blob) cudaFree(plan->blob);
+  delete plan;
+  return FO_OK;
+}
+
+int fo_plan_permutation(const fo_plan* plan, int32_t* perm) {
+  if (!plan || !perm) return fail(FO_E_INVALID, "null argument");
+  std::memcpy(perm, plan->host.perm.data(), sizeof(int32_t) * plan->host.n);
+  return FO_OK;
+}
+
+int fo_workspace_bytes(const fo_plan* plan, int32_t slots, int32_t max_group_cells, size_t* bytes) {
+  if (!plan || !bytes || slots <= 0 || max_group_cells <= 0) return fail(FO_E_INVALID, "bad argument");
+  const int lanes = lanes_for(max_group_cells);
+  *bytes = kHeader + sizeof(double) * (size_t)slots * (size_t)layout_of(plan->host).items * lanes;
+  return FO_OK;
+}
+
+int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
+             int32_t max_group_cells, double* Y, int64_t y_cell_stride, int64_t y_species_stride, const double* k,
+             int64_t k_cell_stride, int64_t k_reaction_stride, const double* atol, double rtol, double dt,
+             double* memory, int64_t* counts, int32_t* status, void* workspace, size_t workspace_bytes,
+             int32_t slots, double* trace, int32_t trace_cap, int32_t* trace_len, void* stream) {
+  if (!plan || !opt || !group_offsets || !Y || !k || !atol || !memory || !counts || !status || !workspace)
+    return fail(FO_E_INVALID, "null argument");
+  if (ngroups <= 0) return FO_OK;
+  if (opt->tableau != FO_TABLEAU_ROS3 && opt->tableau != FO_TABLEAU_RODAS3)
+    return fail(FO_E_INVALID, "unknown tableau");
+  if (max_group_cells <= 0 || max_group_cells > kMaxLanes)
+    return fail(FO_E_UNSUPPORTED, "group size must be 1..256 cells");
+  if (plan->dev.has_constraints) return fail(FO_E_UNSUPPORTED, "constrained (mass = 0) species need the projection");
+  if (!(dt > 0.0)) return fail(FO_E_INVALID, "dt must be positive");
+  if (opt->max_steps < 0) return fail(FO_E_INVALID, "max_steps must be non-negative");
+  const int lanes = lanes_for(max_group_cells);
+  const size_t smem = smem_bytes(plan->host, lanes);
+  int dev = 0, smem_max = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  if (smem > (size_t)smem_max)
+    return fail(FO_E_UNSUPPORTED, "species x group size exceed shared memory: use smaller groups");
+  const int grid = slots > 0 ? (slots < ngroups ? slots : ngroups) : ngroups;
+  size_t need = 0;
+  fo_workspace_bytes(plan, grid, max_group_cells, &need);
+  if (workspace_bytes < need) return fail(FO_E_WORKSPACE, "workspace too small");
+
+  fo::SolveParams p = base_params(plan);
+  p.o.tab = kTableaus[opt->tableau];
+  p.o.controller = opt->controller;
+  p.o.b = opt->b;
+  p.o.safety = opt->safety;
+  p.o.fac_min = opt->fac_min;
+  p.o.fac_max = opt->fac_max;
+  p.o.carry = opt->carry;
+  p.o.quantize = opt->quantize;
+  p.o.carry_memory = opt->carry_memory;
+  p.o.max_steps = opt->max_steps;
+  p.o.k_exp = 3.0;  // embedded order 2 for both tableaus
+  p.ngroups = ngroups;
+  p.group_offsets = group_offsets;
+  p.Y = Y;
+  p.ycs = y_cell_stride;
+  p.yss = y_species_stride;
+  p.k = k;
+  p.kcs = k_cell_stride;
+  p.krs = k_reaction_stride;
+  p.atol = atol;
+  p.rtol = rtol;
+  p.dt = dt;
+  p.memory = memory;
+  p.counts = reinterpret_cast<long long*>(counts);
+  p.status = status;
+  p.lanes = lanes;
+  p.slot_doubles = p.sl.items * lanes;
+  p.scratch = reinterpret_cast<double*>(static_cast<char*>(workspace) + kHeader);
+  p.trace = trace;
+  p.trace_cap = trace ? trace_cap : 0;
+  p.trace_len = trace_len;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (slots > 0) {
+    p.queue = static_cast<int32_t*>(workspace);
+    e = cudaMemsetAsync(workspace, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(queue)");
+  } else {
+    p.queue = nullptr;
+  }
+  e = fo::launch_solve(p, grid, smem, s);
+  if (e != cudaSuccess) return cuda_fail(e, "solve kernel launch");
+  return FO_OK;
+}
+
+static int eval_common(const fo_plan* plan, int32_t C, const double* Y, int64_t ycs, int64_t yss, const double* k,
+                       int64_t kcs, int64_t krs, double* out, int want_jac, void* stream) {
+  if (!plan || !Y || !k || !out) return fail(FO_E_INVALID, "null argument");
+  if (C <= 0) return FO_OK;
+  fo::SolveParams p = base_params(plan);
+  p.Y = const_cast<double*>(Y);
+  p.ycs = ycs;
+  p.yss = yss;
+  p.k = k;
+  p.kcs = kcs;
+  p.krs = krs;
+  p.lanes = 64;
+  p.slot_doubles = p.sl.items * p.lanes;
+  const int blocks = (C + p.lanes - 1) / p.lanes;
+  void* scratch = nullptr;
+  cudaError_t e = cudaMalloc(&scratch, sizeof(double) * (size_t)blocks * p.slot_doubles);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(eval scratch)");
+  p.scratch = static_cast<double*>(scratch);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  e = fo::launch_eval(p, C, want_jac, out, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "eval kernel");
+  return FO_OK;
+}
+
+int fo_eval_rhs(const fo_plan* plan, int32_t C, const double* Y, int64_t ycs, int64_t yss, const double* k,
+                int64_t kcs, int64_t krs, double* F, void* stream) {
+  return eval_common(plan, C, Y, ycs, yss, k, kcs, krs, F, 0, stream);
+}
+
+int fo_eval_jac(const fo_plan* plan, int32_t C, const double* Y, int64_t ycs, int64_t yss, const double* k,
+                int64_t kcs, int64_t krs, double* J, void* stream) {
+  return eval_common(plan, C, Y, ycs, yss, k, kcs, krs, J, 1, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// Device-side data structures shared by the kernels of the integrator.
+#pragma once
+
+#include <cstdint>
+
+namespace fo {
+
+// Index tables of one plan (device pointers), in the permuted numbering.
+struct DevTables {
+  int n, R, P, nlu, nnzj;
+  const int32_t* perm;        // n: original species of permuted index p
+  const double* mass;         // n (permuted)
+  const int32_t* react;       // R*P permuted species, n = a factor of one
+  const int32_t* s_ptr;       // n+1
+  const int32_t* s_rxn;
+  const double* s_val;
+  const int32_t* j_row_ptr;   // n+1
+  const int32_t* j_col;       // nnzj
+  const int32_t* j_src;       // nnzj original pattern entry
+  const int32_t* jt_ptr;      // nnzj+1
+  const int32_t* jt_idx;      // j*P+p
+  const double* jt_val;       // -S[i,j]
+  const int32_t* lu_row_ptr;  // n+1
+  const int32_t* lu_diag;     // n
+  const int32_t* lu_col;      // nlu
+  int has_constraints;
+};
+
+struct DevTableau {
+  double gamma;
+  int S;
+  double a[4][4], c[4][4], m[4], e[4];
+  int new_forcing[4];
+};
+
+struct DevOptions {
+  DevTableau tab;
+  int controller;  // 0 h211b, 1 elementary
+  double b, safety, fac_min, fac_max;
+  int carry, quantize, carry_memory, max_steps;
+  double k_exp;    // embedded order + 1
+};
+
+// Per-lane scratch layout, in items (each item is `lanes` doubles).
+struct ScratchLayout {
+  int64_t lu, negj, d, r, y, ynew, f0, ft, yr, k;  // offsets
+  int64_t items;                                   // total items per lane
+};
+
+struct SolveParams {
+  DevTables t;
+  DevOptions o;
+  ScratchLayout sl;
+  int ngroups;
+  const int32_t* group_offsets;  // device, ngroups+1
+  double* Y;
+  int64_t ycs, yss;
+  const double* k;
+  int64_t kcs, krs;
+  const double* atol;            // original order
+  double rtol, dt;
+  double* memory;
+  long long* counts;
+  int32_t* status;
+  double* scratch;               // per slot: items * lanes doubles
+  int64_t slot_doubles;
+  int32_t* queue;                // work counter (persistent mode) or null
+  int lanes;                     // threads per block (multiple of 32)
+  double* trace;
+  int trace_cap;
+  int32_t* trace_len;
+};
+
+}  // namespace fo

@@ -1,0 +1,505 @@
+// The device integrator: one group of cells per thread block, one cell per
+// thread, the whole interval of fastode.solvers.Algorithm.solve
+// (fastode/solvers.py:305-415) on the device.
+//
+// Mapping. FP64 is the bound on GB300 (about 1 TFLOP/s against 74 TFLOP/s
+// FP32), and a double-precision warp instruction costs the same issue slot
+// whether one lane or all 32 are active. Every lane therefore integrates its
+// own cell with the same instruction stream: the mechanism's pattern, the
+// elimination schedule and the step sequence are shared by the group, so the
+// warp never diverges and no FP64 slot is wasted on masked lanes.
+//
+// Memory. Per-cell working arrays (LU factors, Jacobian values, stage
+// vectors) live in a global scratch slot laid out item-major with cells
+// fastest, so a warp reads one 256-byte line per item. The dense work row of
+// the elimination and the solve vector live in shared memory, indexed
+// [species][lane].
+//
+// Arithmetic order. The stage combinations, the error norm and the
+// controller follow the reference's NumPy expressions operation by operation
+// with explicit round-to-nearest intrinsics (no contraction into FMA), so the
+// step sequence reproduces the reference whenever the two LUs agree to
+// roundoff; the LU, the triangular solves and the sparse map to Jacobian
+// values use FMA.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "device.cuh"
+#include "fastode_gb300.h"
+
+namespace fo {
+
+#define SCR(base, item) (base)[(int64_t)(item) * L + lane]
+#define WROW(c) w[(c) * L + lane]
+
+__device__ __forceinline__ double pymin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double pymax(double a, double b) { return (b > a) ? b : a; }
+// numpy.maximum: NaN if either operand is NaN
+__device__ __forceinline__ double npmax(double a, double b) {
+  if (a != a) return a;
+  if (b != b) return b;
+  return (a > b) ? a : b;
+}
+// numpy.maximum(y, 0.0): keeps NaN, maps -0.0 to 0.0
+__device__ __forceinline__ double clamp0(double y) { return (y <= 0.0) ? 0.0 : y; }
+
+// fastode/solvers.py:46-51
+__device__ __forceinline__ double quantize_step(double h, double interval) {
+  if (h >= interval) return interval;
+  double q = ceil(__dsub_rn(__ddiv_rn(interval, h), 1.0e-9));
+  if (!(q >= 1.0)) q = 1.0;
+  return __ddiv_rn(interval, q);
+}
+
+struct Lane {
+  int lane;      // thread index in the block
+  int L;         // lanes per block
+  int64_t cell;  // global cell index (clamped into the group for idle lanes)
+  bool active;   // this lane owns a real cell of the group
+};
+
+// Rates r_j = k_j * prod(x[react[j, :]]) (fastode/chem.py:86-87).
+__device__ void eval_rates(const SolveParams& p, const Lane& ln, const double* x, double* r) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n, R = p.t.R, P = p.t.P;
+  const double* kc = p.k + ln.cell * p.kcs;
+  for (int j = 0; j < R; ++j) {
+    double prod = 1.0;
+    for (int q = 0; q < P; ++q) {
+      int s = __ldg(p.t.react + j * P + q);
+      if (s != n) prod = __dmul_rn(prod, SCR(x, s));
+    }
+    SCR(r, j) = __dmul_rn(__ldg(kc + (int64_t)j * p.krs), prod);
+  }
+}
+
+// Forcing F = S r, species rows of the permuted stoichiometry
+// (fastode/chem.py:89-90).
+__device__ void eval_forcing(const SolveParams& p, const Lane& ln, const double* r, double* f) {
+  const int L = ln.L, lane = ln.lane;
+  for (int i = 0; i < p.t.n; ++i) {
+    double acc = 0.0;
+    const int q1 = __ldg(p.t.s_ptr + i + 1);
+    for (int q = __ldg(p.t.s_ptr + i); q < q1; ++q)
+      acc = fma(__ldg(p.t.s_val + q), SCR(r, __ldg(p.t.s_rxn + q)), acc);
+    SCR(f, i) = acc;
+  }
+}
+
+__device__ void eval_rhs(const SolveParams& p, const Lane& ln, const double* x, double* r, double* f) {
+  eval_rates(p, ln, x, r);
+  eval_forcing(p, ln, r, f);
+}
+
+// Negated Jacobian values in assembly order: d[j,p] = k_j prod_{q != p} x_q,
+// then -J = sum of (-S[i,j]) d[j,p] over the map's terms
+// (fastode/chem.py:92-102).
+__device__ void eval_negjac(const SolveParams& p, const Lane& ln, const double* x, double* d, double* negj) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n, R = p.t.R, P = p.t.P;
+  const double* kc = p.k + ln.cell * p.kcs;
+  for (int j = 0; j < R; ++j) {
+    const double kj = __ldg(kc + (int64_t)j * p.krs);
+    for (int a = 0; a < P; ++a) {
+      double prod = kj;
+      for (int q = 0; q < P; ++q) {
+        if (q == a) continue;
+        int s = __ldg(p.t.react + j * P + q);
+        if (s != n) prod = __dmul_rn(prod, SCR(x, s));
+      }
+      SCR(d, j * P + a) = prod;
+    }
+  }
+  for (int e = 0; e < p.t.nnzj; ++e) {
+    double acc = 0.0;
+    const int t1 = __ldg(p.t.jt_ptr + e + 1);
+    for (int t = __ldg(p.t.jt_ptr + e); t < t1; ++t)
+      acc = __dadd_rn(acc, __dmul_rn(__ldg(p.t.jt_val + t), SCR(d, __ldg(p.t.jt_idx + t))));
+    SCR(negj, e) = acc;
+  }
+}
+
+// In-place pivot-free LU of alpha*M - J on the precomputed fill pattern,
+// row by row (up-looking). Row r is scattered into the dense work row w,
+// eliminated with the finished rows above it, and gathered back. The
+// diagonal slot keeps the reciprocal of the pivot. Replaces SuperLU's gstrf
+// (fastode/linalg.py:70-78) and LAPACK getrf (fastode/linalg.py:15-18).
+__device__ void factor(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
+                       double* w) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n;
+  const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
+  const int32_t* __restrict__ diag = p.t.lu_diag;
+  const int32_t* __restrict__ col = p.t.lu_col;
+  for (int r = 0; r < n; ++r) {
+    const int q0 = __ldg(rowp + r), q1 = __ldg(rowp + r + 1), dg = __ldg(diag + r);
+    for (int q = q0; q < q1; ++q) WROW(__ldg(col + q)) = 0.0;
+    const int e1 = __ldg(p.t.j_row_ptr + r + 1);
+    for (int e = __ldg(p.t.j_row_ptr + r); e < e1; ++e) WROW(__ldg(p.t.j_col + e)) = SCR(negj, e);
+    WROW(r) = __dadd_rn(WROW(r), __dmul_rn(alpha, __ldg(p.t.mass + r)));
+    for (int q = q0; q < dg; ++q) {
+      const int k = __ldg(col + q);
+      const double l = WROW(k) * SCR(lu, __ldg(diag + k));
+      SCR(lu, q) = l;
+      const int u1 = __ldg(rowp + k + 1);
+      int u = __ldg(diag + k) + 1;
+      for (; u + 3 < u1; u += 4) {
+        const int c0 = __ldg(col + u), c1 = __ldg(col + u + 1), c2 = __ldg(col + u + 2), c3 = __ldg(col + u + 3);
+        const double v0 = SCR(lu, u), v1 = SCR(lu, u + 1), v2 = SCR(lu, u + 2), v3 = SCR(lu, u + 3);
+        WROW(c0) = fma(-l, v0, WROW(c0));
+        WROW(c1) = fma(-l, v1, WROW(c1));
+        WROW(c2) = fma(-l, v2, WROW(c2));
+        WROW(c3) = fma(-l, v3, WROW(c3));
+      }
+      for (; u < u1; ++u) {
+        const int c = __ldg(col + u);
+        WROW(c) = fma(-l, SCR(lu, u), WROW(c));
+      }
+    }
+    SCR(lu, dg) = 1.0 / WROW(r);
+    for (int q = dg + 1; q < q1; ++q) SCR(lu, q) = WROW(__ldg(col + q));
+  }
+}
+
+// Forward and backward substitution in place on w (fastode/linalg.py:80-81).
+__device__ void lu_solve(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n;
+  const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
+  const int32_t* __restrict__ diag = p.t.lu_diag;
+  const int32_t* __restrict__ col = p.t.lu_col;
+  for (int r = 0; r < n; ++r) {
+    double acc = WROW(r);
+    const int dg = __ldg(diag + r);
+    for (int q = __ldg(rowp + r); q < dg; ++q) acc = fma(-SCR(lu, q), WROW(__ldg(col + q)), acc);
+    WROW(r) = acc;
+  }
+  for (int r = n - 1; r >= 0; --r) {
+    double acc = WROW(r);
+    const int dg = __ldg(diag + r), q1 = __ldg(rowp + r + 1);
+    for (int q = dg + 1; q < q1; ++q) acc = fma(-SCR(lu, q), WROW(__ldg(col + q)), acc);
+    WROW(r) = acc * SCR(lu, dg);
+  }
+}
+
+// Sum over the block of one value per thread; every thread gets the same
+// bits (xor butterfly, then the warp totals in warp order).
+__device__ double block_sum(double v, double* red) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  const int nw = blockDim.x >> 5;
+  if (nw == 1) return v;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = red[0];
+  for (int i = 1; i < nw; ++i) s += red[i];
+  return s;
+}
+
+// One attempt's stages (fastode/solvers.py:54-86), then Y_new, the error
+// estimate and this lane's share of the error norm (fastode/solvers.py:37-43).
+__device__ double attempt(const SolveParams& p, const Lane& ln, double H, const double* Y, double* Ynew,
+                          double* scr, double* w, long long& c_rhs, long long& c_solves) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n;
+  const DevTableau& tb = p.o.tab;
+  const bool dae = p.t.has_constraints != 0;
+  double* F0 = scr + p.sl.f0 * L;
+  double* Ft = scr + p.sl.ft * L;
+  double* Yr = scr + p.sl.yr * L;
+  double* K = scr + p.sl.k * L;
+  double* lu = scr + p.sl.lu * L;
+  double* rr = scr + p.sl.r * L;
+  const double* forcing = F0;
+  for (int r = 0; r < tb.S; ++r) {
+    if (r > 0 && tb.new_forcing[r]) {
+      for (int i = 0; i < n; ++i) {
+        double v = SCR(Y, i);
+        for (int s = 0; s < r; ++s)
+          if (tb.a[r][s] != 0.0) v = __dadd_rn(v, __dmul_rn(tb.a[r][s], SCR(K + (int64_t)s * n * L, i)));
+        SCR(Yr, i) = v;
+      }
+      eval_rhs(p, ln, Yr, rr, Ft);
+      ++c_rhs;
+      forcing = Ft;
+    }
+    for (int i = 0; i < n; ++i) {
+      double v = SCR(forcing, i);
+      for (int s = 0; s < r; ++s) {
+        const double coef = __ddiv_rn(tb.c[r][s], H);
+        if (coef != 0.0) {
+          double ks = SCR(K + (int64_t)s * n * L, i);
+          if (dae) ks = __dmul_rn(ks, __ldg(p.t.mass + i));
+          v = __dadd_rn(v, __dmul_rn(coef, ks));
+        }
+      }
+      WROW(i) = v;
+    }
+    lu_solve(p, ln, lu, w);
+    double* Kr = K + (int64_t)r * n * L;
+    for (int i = 0; i < n; ++i) SCR(Kr, i) = WROW(i);
+    ++c_solves;
+  }
+  // Y_new, E and the weighted sum of squares
+  double acc = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double y = SCR(Y, i);
+    double yn = y, e = 0.0;
+    for (int r = 0; r < tb.S; ++r) {
+      const double kv = SCR(K + (int64_t)r * n * L, i);
+      if (tb.m[r] != 0.0) yn = __dadd_rn(yn, __dmul_rn(tb.m[r], kv));
+      if (tb.e[r] != 0.0) e = __dadd_rn(e, __dmul_rn(tb.e[r], kv));
+    }
+    SCR(Ynew, i) = yn;
+    const double ymax = npmax(fabs(y), fabs(yn));
+    const double s = __ddiv_rn(e, __dadd_rn(__ldg(p.atol + __ldg(p.t.perm + i)), __dmul_rn(p.rtol, ymax)));
+    acc = __dadd_rn(acc, __dmul_rn(s, s));
+  }
+  return ln.active ? acc : 0.0;
+}
+
+__device__ void trace_record(const SolveParams& p, int g, int& nrec, double t, double H, double err, double outcome) {
+  if (p.trace == nullptr || threadIdx.x != 0) {
+    ++nrec;
+    return;
+  }
+  if (nrec < p.trace_cap) {
+    double* rec = p.trace + ((int64_t)g * p.trace_cap + nrec) * 4;
+    rec[0] = t;
+    rec[1] = H;
+    rec[2] = err;
+    rec[3] = outcome;
+  }
+  ++nrec;
+}
+
+// One group over one interval: fastode/solvers.py:305-415 statement by statement.
+__device__ void solve_group(const SolveParams& p, int g, double* scr, double* w, double* red) {
+  const int L = blockDim.x, lane = threadIdx.x;
+  const int n = p.t.n;
+  const int64_t c0 = p.group_offsets[g], c1 = p.group_offsets[g + 1];
+  const int64_t C = c1 - c0;
+  Lane ln;
+  ln.lane = lane;
+  ln.L = L;
+  ln.active = lane < C;
+  ln.cell = c0 + (ln.active ? lane : (C - 1));
+  const DevOptions& o = p.o;
+  const double dt = p.dt;
+
+  long long c_steps = 0, c_acc = 0, c_rej = 0, c_rhs = 0, c_jac = 0, c_lu = 0, c_solves = 0;
+  int nrec = 0;
+
+  double* Y = scr + p.sl.y * L;
+  double* Ynew = scr + p.sl.ynew * L;
+  double* F0 = scr + p.sl.f0 * L;
+  double* negj = scr + p.sl.negj * L;
+  double* dd = scr + p.sl.d * L;
+  double* rr = scr + p.sl.r * L;
+  double* lu = scr + p.sl.lu * L;
+
+  for (int i = 0; i < n; ++i) SCR(Y, i) = p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss];
+
+  double* mem = p.memory + (int64_t)g * 3;
+  double h_next = mem[0], err_prev = mem[1], h_prev = mem[2];
+  if (!(o.carry && o.carry_memory)) err_prev = h_prev = 0.0;
+  const double h_min = __dmul_rn(1.0e-15, dt);
+  const double h_max = dt;
+  double H = (o.carry && h_next > 0.0) ? h_next : __dmul_rn(1.0e-6, dt);
+  H = pymin(pymax(h_min, H), h_max);
+  if (o.quantize) H = quantize_step(H, dt);
+  double proposed = H;
+  const double elem_exp = 1.0 / o.k_exp;
+  const double up = 1.0 + 1.0e-8, down = 1.0 - 1.0e-8;
+  const double rounding = 2.220446049250313e-16;
+
+  double t = 0.0;
+  bool reject_last = false, reject_more = false;
+  int nsteps = 0;
+  int status = -1;  // running
+  const double nsize = (double)(C * n);
+  while (__dadd_rn(__dsub_rn(t, dt), rounding) <= 0.0 && status < 0) {
+    if (nsteps >= o.max_steps) {
+      status = FO_STATUS_TOO_MANY_STEPS;
+      break;
+    }
+    if (__dadd_rn(t, __dmul_rn(0.1, H)) == t || H < h_min) {
+      status = FO_STATUS_STEP_TOO_SMALL;
+      break;
+    }
+    bool last = __dsub_rn(dt, t) <= __dmul_rn(H, up);
+    bool shortened = last && __dsub_rn(dt, t) < __dmul_rn(H, down);
+    double H_ctrl = H;
+    if (last) H = __dsub_rn(dt, t);
+    eval_rhs(p, ln, Y, rr, F0);
+    ++c_rhs;
+    eval_negjac(p, ln, Y, dd, negj);
+    ++c_jac;
+    bool accepted = false;
+    while (!accepted) {
+      if (nsteps >= o.max_steps) {
+        status = FO_STATUS_TOO_MANY_STEPS;
+        break;
+      }
+      if (H < h_min || __dadd_rn(t, __dmul_rn(0.1, H)) == t) {
+        status = FO_STATUS_STEP_TOO_SMALL;
+        break;
+      }
+      factor(p, ln, 1.0 / __dmul_rn(H, o.tab.gamma), negj, lu, w);
+      ++c_lu;
+      const double part = attempt(p, ln, H, Y, Ynew, scr, w, c_rhs, c_solves);
+      const double total = block_sum(part, red);
+      double err = sqrt(__ddiv_rn(total, nsize));
+      if (!isnan(err)) err = pymax(err, 1.0e-10);
+      ++nsteps;
+      ++c_steps;
+      if (isnan(err) || isinf(err)) {
+        trace_record(p, g, nrec, t, H, err, -1.0);
+        status = FO_STATUS_NAN_OR_INF;
+        break;
+      }
+      if (err < 1.0 && shortened) {
+        trace_record(p, g, nrec, t, H, err, 1.0);
+        ++c_acc;
+        t = dt;
+        double* tmp = Y; Y = Ynew; Ynew = tmp;
+        proposed = H_ctrl;
+        accepted = true;
+      } else if (err < 1.0) {
+        trace_record(p, g, nrec, t, H, err, 1.0);
+        // fastode/solvers.py:297-303
+        double fac = __ddiv_rn(o.safety, pow(err, elem_exp));
+        if (o.controller == FO_CONTROLLER_H211B && err_prev > 0.0 && h_prev > 0.0) {
+          fac = __dmul_rn(__dmul_rn(o.safety, pow(__dmul_rn(err, err_prev), -1.0 / __dmul_rn(o.b, o.k_exp))),
+                          pow(__ddiv_rn(H, h_prev), -1.0 / o.b));
+        }
+        fac = pymin(o.fac_max, pymax(o.fac_min, fac));
+        ++c_acc;
+        t = last ? dt : __dadd_rn(t, H);
+        double* tmp = Y; Y = Ynew; Ynew = tmp;
+        err_prev = err;
+        h_prev = H;
+        double Hnew = __dmul_rn(H, fac);
+        if (reject_last) Hnew = pymin(Hnew, H);
+        Hnew = pymax(h_min, pymin(Hnew, h_max));
+        if (o.quantize) Hnew = quantize_step(Hnew, dt);
+        reject_last = reject_more = false;
+        proposed = Hnew;
+        H = Hnew;
+        accepted = true;
+      } else {
+        trace_record(p, g, nrec, t, H, err, 0.0);
+        double Hnew = __dmul_rn(H, pymax(o.fac_min, __ddiv_rn(o.safety, pow(err, elem_exp))));
+        if (reject_more) Hnew = __dmul_rn(H, 0.1);
+        reject_more = reject_last;
+        reject_last = true;
+        if (o.quantize) Hnew = quantize_step(Hnew, dt);
+        H = Hnew;
+        last = __dsub_rn(dt, t) <= __dmul_rn(H, up);
+        shortened = last && __dsub_rn(dt, t) < __dmul_rn(H, down);
+        H_ctrl = H;
+        if (last) H = __dsub_rn(dt, t);
+        ++c_rej;
+      }
+    }
+  }
+  if (status < 0) status = FO_STATUS_CONVERGED;
+
+  // clamp (fastode/solvers.py:89-97) and write back
+  if (ln.active) {
+    for (int i = 0; i < n; ++i) {
+      double y = SCR(Y, i);
+      if (!p.t.has_constraints || __ldg(p.t.mass + i) == 1.0) y = clamp0(y);
+      p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss] = y;
+    }
+  }
+  if (threadIdx.x == 0) {
+    mem[0] = proposed;
+    mem[1] = err_prev;
+    mem[2] = h_prev;
+    long long* cn = p.counts + (int64_t)g * FO_NUM_COUNTS;
+    cn[0] += c_steps;
+    cn[1] += c_acc;
+    cn[2] += c_rej;
+    cn[3] += c_rhs;
+    cn[4] += c_jac;
+    cn[5] += c_lu;
+    cn[6] += c_solves;
+    cn[12] += 1;
+    p.status[g] = status;
+    if (p.trace_len) p.trace_len[g] = nrec;
+  }
+}
+
+__global__ void __launch_bounds__(256) solve_kernel(SolveParams p) {
+  extern __shared__ double smem[];
+  double* red = smem;       // 32 doubles
+  double* w = smem + 32;    // n * lanes
+  double* scr = p.scratch + (int64_t)blockIdx.x * p.slot_doubles;
+  if (p.queue == nullptr) {
+    solve_group(p, blockIdx.x, scr, w, red);
+    return;
+  }
+  __shared__ int next;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) next = atomicAdd(p.queue, 1);
+    __syncthreads();
+    const int g = next;
+    if (g >= p.ngroups) break;
+    solve_group(p, g, scr, w, red);
+  }
+}
+
+// ---- standalone evaluations (fastode/chem.py:86-102) ------------------------
+
+__global__ void eval_kernel(SolveParams p, int C, int want_jac, double* out) {
+  const int L = blockDim.x, lane = threadIdx.x;
+  const int64_t cell = (int64_t)blockIdx.x * L + lane;
+  Lane ln;
+  ln.lane = lane;
+  ln.L = L;
+  ln.active = cell < C;
+  ln.cell = ln.active ? cell : (C - 1);
+  double* scr = p.scratch + (int64_t)blockIdx.x * p.slot_doubles;
+  const int n = p.t.n;
+  double* Y = scr + p.sl.y * L;
+  for (int i = 0; i < n; ++i) SCR(Y, i) = p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss];
+  if (!want_jac) {
+    double* f = scr + p.sl.f0 * L;
+    eval_rhs(p, ln, Y, scr + p.sl.r * L, f);
+    if (ln.active)
+      for (int i = 0; i < n; ++i) out[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss] = SCR(f, i);
+  } else {
+    double* negj = scr + p.sl.negj * L;
+    eval_negjac(p, ln, Y, scr + p.sl.d * L, negj);
+    if (ln.active)
+      for (int e = 0; e < p.t.nnzj; ++e) out[ln.cell * p.t.nnzj + __ldg(p.t.j_src + e)] = -SCR(negj, e);
+  }
+}
+
+#undef SCR
+#undef WROW
+
+// ---- launch wrappers ----------------------------------------------------------
+
+cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream) {
+  static int configured_smem = -1;
+  if ((int)smem > 48 * 1024 && (int)smem != configured_smem) {
+    cudaError_t e = cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured_smem = (int)smem;
+  }
+  solve_kernel<<<grid, p.lanes, smem, stream>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eval(const SolveParams& p, int C, int want_jac, double* out, cudaStream_t stream) {
+  const int blocks = (C + p.lanes - 1) / p.lanes;
+  eval_kernel<<<blocks, p.lanes, 0, stream>>>(p, C, want_jac, out);
+  return cudaGetLastError();
+}
+
+}  // namespace fo

@@ -1,0 +1,310 @@
+// Symbolic analysis for the pivot-free batched sparse LU.
+//
+// The reference factors alpha*M - J of a whole group with SuperLU and the
+// MMD_AT_PLUS_A column ordering, from scratch on every attempt
+// (fastode/linalg.py:70-78), with partial pivoting. Here the ordering and the
+// fill pattern are computed once per mechanism: the same pattern serves every
+// cell and every attempt, so the device runs a fixed, branch-free elimination.
+// Pivoting is dropped, as MICM's LuDecompositionMozartInPlace (the reference's
+// validated baseline, validation/micm_scenario.cpp:46-51) drops it; the stage
+// matrix of a stiff chemistry system is dominated by its diagonal.
+#include "symbolic.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <queue>
+#include <set>
+
+namespace fo {
+
+std::string validate(const fo_mechanism_desc& m) {
+  if (m.n <= 0) return "n must be positive";
+  if (m.R < 0) return "R must be non-negative";
+  if (m.P <= 0) return "P must be positive";
+  if (m.nnz < m.n) return "the Jacobian pattern must hold the diagonal";
+  if (!m.pat_rows || !m.pat_cols) return "missing Jacobian pattern";
+  if (m.R > 0 && (!m.react || !m.s_indptr || !m.j_indptr)) return "missing reaction tables";
+  if (!m.s_indptr) return "missing stoichiometry";
+  for (int64_t q = 0; q < (int64_t)m.R * m.P; ++q)
+    if (m.react[q] < 0 || m.react[q] > m.n) return "reactant index out of range";
+  if (m.s_indptr[0] != 0) return "stoichiometry indptr must start at 0";
+  for (int i = 0; i < m.n; ++i)
+    if (m.s_indptr[i + 1] < m.s_indptr[i]) return "stoichiometry indptr must be non-decreasing";
+  for (int q = 0; q < m.s_indptr[m.n]; ++q)
+    if (m.s_idx[q] < 0 || m.s_idx[q] >= m.R) return "stoichiometry reaction index out of range";
+  std::vector<char> diag(m.n, 0);
+  for (int e = 0; e < m.nnz; ++e) {
+    if (m.pat_rows[e] < 0 || m.pat_rows[e] >= m.n || m.pat_cols[e] < 0 || m.pat_cols[e] >= m.n)
+      return "pattern index out of range";
+    if (m.pat_rows[e] == m.pat_cols[e]) diag[m.pat_rows[e]] = 1;
+  }
+  for (int i = 0; i < m.n; ++i)
+    if (!diag[i]) return "the Jacobian pattern must hold every diagonal entry";
+  if (m.j_indptr) {
+    if (m.j_indptr[0] != 0) return "Jacobian map indptr must start at 0";
+    for (int e = 0; e < m.nnz; ++e)
+      if (m.j_indptr[e + 1] < m.j_indptr[e]) return "Jacobian map indptr must be non-decreasing";
+    for (int q = 0; q < m.j_indptr[m.nnz]; ++q)
+      if (m.j_idx[q] < 0 || m.j_idx[q] >= m.R * m.P) return "Jacobian map column out of range";
+  }
+  return "";
+}
+
+int64_t symbolic_lu(int n, const std::vector<std::vector<int>>& pat, std::vector<std::vector<int>>* rows,
+                    int* nnz_l, int* nnz_u) {
+  // Row-by-row (up-looking) symbolic elimination: row i's final pattern is its
+  // own pattern united with U(k) for every k < i that ends up in L(i).
+  std::vector<std::vector<int>> U(n);
+  std::vector<int> mark(n, -1);
+  int64_t fma = 0;
+  int nl = 0, nu = 0;
+  if (rows) rows->assign(n, {});
+  for (int i = 0; i < n; ++i) {
+    std::vector<int> members;
+    std::priority_queue<int, std::vector<int>, std::greater<int>> lower;
+    auto add = [&](int c) {
+      if (mark[c] == i) return;
+      mark[c] = i;
+      members.push_back(c);
+      if (c < i) lower.push(c);
+    };
+    add(i);
+    for (int c : pat[i]) add(c);
+    while (!lower.empty()) {
+      int k = lower.top();
+      lower.pop();
+      fma += (int64_t)U[k].size();
+      for (int j : U[k]) add(j);
+    }
+    std::sort(members.begin(), members.end());
+    for (int c : members) {
+      if (c < i) ++nl;
+      if (c > i) {
+        ++nu;
+        U[i].push_back(c);
+      }
+    }
+    if (rows) (*rows)[i] = members;
+  }
+  if (nnz_l) *nnz_l = nl;
+  if (nnz_u) *nnz_u = nu;
+  return fma;
+}
+
+namespace {
+
+struct Bitset {
+  int words = 0;
+  std::vector<uint64_t> bits;
+  void init(int n, int count) {
+    words = (n + 63) / 64;
+    bits.assign((size_t)words * count, 0);
+  }
+  uint64_t* row(int i) { return bits.data() + (size_t)i * words; }
+};
+
+int popcnt(uint64_t x) { return __builtin_popcountll(x); }
+
+// Greedy elimination on the symmetric graph of A + A^T. mode 0: minimum
+// degree; mode 1: minimum fill among the `window` lowest-degree vertices.
+// Ties go to the lowest degree, then the lowest index.
+std::vector<int> greedy_order(int n, const std::vector<std::vector<int>>& adj_in, int mode, int window) {
+  Bitset g;
+  g.init(n, n);
+  for (int i = 0; i < n; ++i)
+    for (int j : adj_in[i])
+      if (i != j) {
+        g.row(i)[j / 64] |= 1ull << (j % 64);
+        g.row(j)[i / 64] |= 1ull << (i % 64);
+      }
+  std::vector<char> alive(n, 1);
+  std::vector<int> degree(n, 0), order;
+  order.reserve(n);
+  auto deg = [&](int v) {
+    int d = 0;
+    uint64_t* r = g.row(v);
+    for (int w = 0; w < g.words; ++w) d += popcnt(r[w]);
+    return d;
+  };
+  for (int v = 0; v < n; ++v) degree[v] = deg(v);
+  std::vector<int> nb;
+  for (int step = 0; step < n; ++step) {
+    int best = -1;
+    if (mode == 0) {
+      for (int v = 0; v < n; ++v)
+        if (alive[v] && (best < 0 || degree[v] < degree[best])) best = v;
+    } else {
+      std::vector<int> cand;
+      for (int v = 0; v < n; ++v)
+        if (alive[v]) cand.push_back(v);
+      std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return degree[a] < degree[b]; });
+      if ((int)cand.size() > window) cand.resize(window);
+      int64_t best_fill = -1;
+      for (int v : cand) {
+        uint64_t* rv = g.row(v);
+        int64_t fill = 0;
+        for (int w = 0; w < g.words; ++w) {
+          uint64_t x = rv[w];
+          while (x) {
+            int a = w * 64 + __builtin_ctzll(x);
+            x &= x - 1;
+            uint64_t* ra = g.row(a);
+            for (int u = 0; u < g.words; ++u) fill += popcnt(rv[u] & ~ra[u]);
+            fill -= 1;  // a itself
+          }
+        }
+        if (best < 0 || fill < best_fill || (fill == best_fill && degree[v] < degree[best])) {
+          best = v;
+          best_fill = fill;
+        }
+      }
+    }
+    order.push_back(best);
+    alive[best] = 0;
+    nb.clear();
+    uint64_t* rb = g.row(best);
+    for (int w = 0; w < g.words; ++w) {
+      uint64_t x = rb[w];
+      while (x) {
+        nb.push_back(w * 64 + __builtin_ctzll(x));
+        x &= x - 1;
+      }
+    }
+    for (int a : nb) {
+      uint64_t* ra = g.row(a);
+      for (int w = 0; w < g.words; ++w) ra[w] |= rb[w];
+      ra[a / 64] &= ~(1ull << (a % 64));
+      ra[best / 64] &= ~(1ull << (best % 64));
+    }
+    std::fill(rb, rb + g.words, 0ull);
+    for (int a : nb) degree[a] = deg(a);
+  }
+  return order;
+}
+
+std::vector<std::vector<int>> permuted_pattern(const fo_mechanism_desc& m, const std::vector<int>& iperm) {
+  std::vector<std::vector<int>> pat(m.n);
+  for (int e = 0; e < m.nnz; ++e) pat[iperm[m.pat_rows[e]]].push_back(iperm[m.pat_cols[e]]);
+  return pat;
+}
+
+int64_t cost_of(const fo_mechanism_desc& m, const std::vector<int>& order) {
+  std::vector<int> iperm(m.n);
+  for (int p = 0; p < m.n; ++p) iperm[order[p]] = p;
+  return symbolic_lu(m.n, permuted_pattern(m, iperm), nullptr, nullptr, nullptr);
+}
+
+}  // namespace
+
+std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t) {
+  std::string err = validate(m);
+  if (!err.empty()) return err;
+  const int n = m.n, R = m.R, P = m.P;
+  t->n = n;
+  t->R = R;
+  t->P = P;
+  t->nnz = m.nnz;
+
+  // symmetric structure for the orderings
+  std::vector<std::vector<int>> adj(n);
+  for (int e = 0; e < m.nnz; ++e) adj[m.pat_rows[e]].push_back((int)m.pat_cols[e]);
+
+  std::vector<int> natural(n);
+  std::iota(natural.begin(), natural.end(), 0);
+  std::vector<std::pair<int, std::vector<int>>> cands;
+  if (ordering == FO_ORDER_NATURAL || ordering == FO_ORDER_AUTO) cands.push_back({FO_ORDER_NATURAL, natural});
+  if (ordering == FO_ORDER_MIN_DEGREE || ordering == FO_ORDER_AUTO)
+    cands.push_back({FO_ORDER_MIN_DEGREE, greedy_order(n, adj, 0, 0)});
+  if (ordering == FO_ORDER_MIN_FILL || ordering == FO_ORDER_AUTO) {
+    cands.push_back({FO_ORDER_MIN_FILL, greedy_order(n, adj, 1, n <= 400 ? n : 32)});
+    if (ordering == FO_ORDER_AUTO && n > 8) cands.push_back({FO_ORDER_MIN_FILL, greedy_order(n, adj, 1, 8)});
+  }
+  if (cands.empty()) return "unknown ordering";
+  int best = 0;
+  int64_t best_cost = -1;
+  for (size_t c = 0; c < cands.size(); ++c) {
+    int64_t cost = cost_of(m, cands[c].second);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = (int)c;
+    }
+  }
+  t->ordering = cands[best].first;
+  t->perm.assign(cands[best].second.begin(), cands[best].second.end());
+  t->iperm.assign(n, 0);
+  for (int p = 0; p < n; ++p) t->iperm[t->perm[p]] = p;
+
+  t->mass.assign(n, 1.0);
+  if (m.mass)
+    for (int p = 0; p < n; ++p) t->mass[p] = m.mass[t->perm[p]];
+
+  // rates
+  t->react.assign((size_t)R * P, n);
+  for (int j = 0; j < R; ++j)
+    for (int p = 0; p < P; ++p) {
+      int64_t s = m.react[(size_t)j * P + p];
+      t->react[(size_t)j * P + p] = s == n ? n : t->iperm[s];
+    }
+  // stoichiometry rows in permuted order
+  t->s_ptr.assign(1, 0);
+  t->s_rxn.clear();
+  t->s_val.clear();
+  for (int p = 0; p < n; ++p) {
+    int i = t->perm[p];
+    for (int q = m.s_indptr[i]; q < m.s_indptr[i + 1]; ++q) {
+      t->s_rxn.push_back(m.s_idx[q]);
+      t->s_val.push_back(m.s_val[q]);
+    }
+    t->s_ptr.push_back((int32_t)t->s_rxn.size());
+  }
+
+  // LU structure
+  std::vector<std::vector<int>> pat = permuted_pattern(m, t->iperm);
+  std::vector<std::vector<int>> rows;
+  t->lu_fma = symbolic_lu(n, pat, &rows, &t->nnz_l, &t->nnz_u);
+  t->solve_fma = (int64_t)t->nnz_l + t->nnz_u;
+  t->lu_row_ptr.assign(1, 0);
+  t->lu_diag.assign(n, 0);
+  t->lu_col.clear();
+  for (int r = 0; r < n; ++r) {
+    for (int c : rows[r]) {
+      if (c == r) t->lu_diag[r] = (int32_t)t->lu_col.size();
+      t->lu_col.push_back(c);
+    }
+    t->lu_row_ptr.push_back((int32_t)t->lu_col.size());
+  }
+
+  // Jacobian entries in assembly order
+  std::vector<std::vector<std::pair<int, int>>> by_row(n);  // (perm col, original entry)
+  for (int e = 0; e < m.nnz; ++e)
+    by_row[t->iperm[m.pat_rows[e]]].push_back({t->iperm[m.pat_cols[e]], e});
+  t->j_row_ptr.assign(1, 0);
+  t->j_col.clear();
+  t->j_src.clear();
+  t->j_lu_pos.clear();
+  t->jt_ptr.assign(1, 0);
+  t->jt_idx.clear();
+  t->jt_val.clear();
+  for (int r = 0; r < n; ++r) {
+    std::sort(by_row[r].begin(), by_row[r].end());
+    for (auto& ce : by_row[r]) {
+      int c = ce.first, e = ce.second;
+      t->j_col.push_back(c);
+      t->j_src.push_back(e);
+      auto b = t->lu_col.begin() + t->lu_row_ptr[r], en = t->lu_col.begin() + t->lu_row_ptr[r + 1];
+      auto it = std::lower_bound(b, en, c);
+      t->j_lu_pos.push_back((int32_t)(it - t->lu_col.begin()));
+      if (m.j_indptr)
+        for (int q = m.j_indptr[e]; q < m.j_indptr[e + 1]; ++q) {
+          t->jt_idx.push_back(m.j_idx[q]);
+          t->jt_val.push_back(-m.j_val[q]);
+        }
+      t->jt_ptr.push_back((int32_t)t->jt_idx.size());
+    }
+    t->j_row_ptr.push_back((int32_t)t->j_col.size());
+  }
+  return "";
+}
+
+}  // namespace fo

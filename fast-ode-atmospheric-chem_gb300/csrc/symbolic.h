@@ -1,0 +1,57 @@
+// Host-side symbolic analysis of a mass-action mechanism: fill-reducing
+// ordering, pivot-free sparse LU structure and the index tables the device
+// integrator walks. No CUDA here; the plan's tables are uploaded by abi.cu.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fastode_gb300.h"
+
+namespace fo {
+
+// Everything the device needs, in the permuted species numbering
+// (p = 0..n-1 is the p-th eliminated species, perm[p] its original index).
+struct HostTables {
+  int n = 0, R = 0, P = 0, nnz = 0;
+  int ordering = 0;
+  std::vector<int32_t> perm, iperm;
+  std::vector<double> mass;            // permuted
+
+  // rates: react_p[j*P+p] = permuted species or n (a factor of one)
+  std::vector<int32_t> react;
+  // stoichiometry rows in permuted order: (reaction, coefficient)
+  std::vector<int32_t> s_ptr, s_rxn;
+  std::vector<double> s_val;
+
+  // Jacobian values in assembly order (permuted row-major):
+  // entry q sits in permuted row r with j_row_ptr[r] <= q < j_row_ptr[r+1],
+  // permuted column j_col[q], original pattern entry j_src[q]
+  std::vector<int32_t> j_row_ptr, j_col, j_src;
+  // value map of entry q: terms jt_ptr[q]..jt_ptr[q+1], jp index and -S[i,j]
+  std::vector<int32_t> jt_ptr, jt_idx;
+  std::vector<double> jt_val;
+
+  // LU storage: row r holds L entries (columns < r, ascending), the diagonal,
+  // then U entries (columns > r, ascending)
+  std::vector<int32_t> lu_row_ptr, lu_diag, lu_col;
+  // position of the Jacobian entry q inside the LU storage
+  std::vector<int32_t> j_lu_pos;
+
+  int64_t lu_fma = 0, solve_fma = 0;
+  int nnz_l = 0, nnz_u = 0;
+};
+
+// Validate a descriptor; returns an empty string when it is consistent.
+std::string validate(const fo_mechanism_desc& m);
+
+// Symbolic LU for a given elimination order; returns the multiply-add count
+// and fills the row structure when `rows` is non-null.
+int64_t symbolic_lu(int n, const std::vector<std::vector<int>>& pattern_rows_perm,
+                    std::vector<std::vector<int>>* rows, int* nnz_l, int* nnz_u);
+
+// Build all tables (ordering FO_ORDER_*).
+std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t);
+
+}  // namespace fo

@@ -1,0 +1,199 @@
+/*
+ * fastode_gb300 — C-ABI of the GB300 Rosenbrock integrator for mass-action
+ * chemistry (FP64, sm_103a).
+ *
+ * This header is the drop-in boundary for the reference package fastode
+ * (davidfillmore/Fast-ODE-Atmospheric-Chem). Each entry point names the
+ * reference interface it replaces. All functions return an int status
+ * (FO_OK = 0 or a negative FO_E* code) and never abort; numerical failures
+ * of an integration are reported per group in the status array, with the
+ * codes of FO_STATUS_*, exactly as the reference returns status strings.
+ *
+ * Data layout on the device: a state array Y holds n species x C cells and a
+ * rate-constant array k holds R reactions x C cells. Both are addressed by
+ * two strides (in doubles): element (cell c, species s) is at
+ * Y[c * y_cell_stride + s * y_species_stride]. The batched layout is
+ * species-major with cells fastest (cell stride 1, species stride C), which
+ * makes every warp access a coalesced 256-byte line; the reference's (C, n)
+ * row-major layout is cell stride n, species stride 1.
+ *
+ * Pointers marked "device" must be device memory (cudaMalloc or a torch CUDA
+ * tensor); "host" pointers are host memory. The stream argument is a
+ * cudaStream_t passed as void* (0 = legacy default stream).
+ */
+#ifndef FASTODE_GB300_H
+#define FASTODE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FO_OK 0
+#define FO_E_INVALID (-1)      /* bad argument */
+#define FO_E_CUDA (-2)         /* a CUDA runtime call failed */
+#define FO_E_UNSUPPORTED (-3)  /* size or option outside what the kernels handle */
+#define FO_E_WORKSPACE (-4)    /* workspace too small */
+#define FO_E_ALLOC (-5)        /* host allocation failed */
+
+/* Per-group integration status; the strings are those of fastode/solvers.py:305-415. */
+#define FO_STATUS_CONVERGED 0          /* "converged" */
+#define FO_STATUS_TOO_MANY_STEPS 1     /* "too many steps" */
+#define FO_STATUS_STEP_TOO_SMALL 2     /* "step too small" */
+#define FO_STATUS_NAN_OR_INF 3         /* "nan or inf" */
+#define FO_STATUS_PROJECTION_FAILED 4  /* "projection failed" */
+
+/* Number and order of the per-group counters (fastode/counts.py:10-23):
+ * steps, accepted, rejected, rhs, jac, lu, solves, newton, failures,
+ * unconverged, proj_passes, proj_trials, calls. */
+#define FO_NUM_COUNTS 13
+
+/* Tableaus (fastode/tableaus.py:70-90). */
+#define FO_TABLEAU_ROS3 0
+#define FO_TABLEAU_RODAS3 1
+
+/* Step-size controllers of fastode/solvers.py:297-303. */
+#define FO_CONTROLLER_H211B 0
+#define FO_CONTROLLER_ELEMENTARY 1
+
+/* Fill-reducing orderings for the pivot-free sparse LU. */
+#define FO_ORDER_AUTO 0          /* the one of the candidates below with the fewest LU flops */
+#define FO_ORDER_NATURAL 1
+#define FO_ORDER_MIN_DEGREE 2
+#define FO_ORDER_MIN_FILL 3
+
+/*
+ * A compiled mechanism, as fastode.chem.Mechanism builds it
+ * (fastode/chem.py:19-79): reactant table, stoichiometry, Jacobian pattern
+ * and the sparse map from rate partials to Jacobian values. All host pointers.
+ */
+typedef struct fo_mechanism_desc {
+  int32_t n;                  /* species */
+  int32_t R;                  /* reactions */
+  int32_t P;                  /* reactant slots per reaction */
+  const int64_t* react;       /* R*P row-major species indices; n pads a slot (a factor of one) */
+  const int32_t* s_indptr;    /* n+1: stoichiometry rows S[i, :] in CSR */
+  const int32_t* s_idx;       /* reaction index of each nonzero */
+  const double* s_val;        /* S[i, j] */
+  int32_t nnz;                /* Jacobian pattern entries (diagonal included) */
+  const int64_t* pat_rows;    /* nnz */
+  const int64_t* pat_cols;    /* nnz */
+  const int32_t* j_indptr;    /* nnz+1: Jacobian-value map in CSR over entries (the GT map) */
+  const int32_t* j_idx;       /* j*P + p of each term */
+  const double* j_val;        /* coefficient S[i, j] of each term */
+  const double* mass;         /* n: 1 differential, 0 algebraic (may be NULL: all ones) */
+} fo_mechanism_desc;
+
+/* What the symbolic analysis found (host-side, no GPU needed). */
+typedef struct fo_plan_info {
+  int32_t n, R, P, nnz_jac;
+  int32_t ordering;           /* the FO_ORDER_* actually used */
+  int32_t nnz_lu;             /* entries of L+U including the diagonal (pattern plus fill) */
+  int32_t nnz_l, nnz_u;       /* strictly lower / strictly upper entries */
+  int64_t lu_fma;             /* multiply-adds of one factorization */
+  int64_t solve_fma;          /* multiply-adds of one forward+backward solve */
+  int32_t jac_terms;          /* terms of the Jacobian-value map */
+  int32_t stoich_nnz;         /* nonzeros of S */
+  int64_t scratch_doubles_per_cell;  /* per-cell device scratch of the integrator */
+  int32_t smem_doubles_per_cell;     /* per-cell shared memory of the integrator */
+} fo_plan_info;
+
+typedef struct fo_plan fo_plan;  /* opaque */
+
+/* Integrator options: the constructor arguments of fastode.Algorithm
+ * (fastode/solvers.py:275-292). */
+typedef struct fo_options {
+  int32_t tableau;            /* FO_TABLEAU_* */
+  int32_t controller;         /* FO_CONTROLLER_* ("h211b" or anything else = elementary) */
+  double b;                   /* filter parameter (4) */
+  double safety;              /* 0.9 */
+  double fac_min;             /* 0.2 */
+  double fac_max;             /* 6 */
+  int32_t carry;              /* start from the carried proposal */
+  int32_t quantize;           /* round proposals to divisors of the interval */
+  int32_t carry_memory;       /* keep the filter memory across intervals */
+  int32_t max_steps;          /* attempt budget per call (1000) */
+} fo_options;
+
+/* Host-only symbolic analysis: ordering, fill and flop counts, and (when
+ * perm is not NULL) the elimination order perm[p] = species eliminated p-th.
+ * Replaces the ordering step of SuperLU's splu(permc_spec="MMD_AT_PLUS_A")
+ * that fastode/linalg.py:70-78 runs on every factorization. Needs no GPU. */
+int fo_analyze(const fo_mechanism_desc* mech, int32_t ordering, fo_plan_info* info, int32_t* perm);
+
+/* Build a plan: symbolic analysis on the host, then the index tables are
+ * copied to the current CUDA device. Replaces fastode.chem.Mechanism's
+ * compiled tables (fastode/chem.py:19-79) plus linalg.SparsePattern
+ * (fastode/linalg.py:32-67) as the device sees them. */
+int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** plan);
+int fo_plan_info_get(const fo_plan* plan, fo_plan_info* info);
+int fo_plan_destroy(fo_plan* plan);
+
+/* The permutation chosen by the ordering: perm[p] = species eliminated p-th (host, n). */
+int fo_plan_permutation(const fo_plan* plan, int32_t* perm);
+
+/* Bytes of device workspace fo_solve needs for `slots` groups in flight
+ * of at most `max_group_cells` cells each (see fo_solve). */
+int fo_workspace_bytes(const fo_plan* plan, int32_t slots, int32_t max_group_cells, size_t* bytes);
+
+/*
+ * Integrate every group over one interval of length dt: the device form of
+ * fastode.solvers.Algorithm.solve(system, Y, dt, atol, rtol, counts, memory)
+ * (fastode/solvers.py:305-415), for many groups at once.
+ *
+ * Group g holds cells [group_offsets[g], group_offsets[g+1]) and shares one
+ * step sequence, one error norm and one controller memory, as a group of C
+ * cells shares them in the reference. group_offsets (device, ngroups+1) must
+ * be increasing; no group may hold more than max_group_cells cells, and
+ * max_group_cells may be 1..256 (n * roundup32(max_group_cells) doubles must
+ * fit in shared memory).
+ *
+ * Y          device, in/out, updated in place to the clamped result.
+ * k          device, rate constants (C x R via the two k strides).
+ * atol       device, n doubles (species order of the mechanism).
+ * memory     device, ngroups x 3 doubles (h_next, err_prev, h_prev) in/out
+ *            (fastode/solvers.py:181-186 Memory).
+ * counts     device, ngroups x FO_NUM_COUNTS int64, ACCUMULATED (+=).
+ * status     device, ngroups int32, written (FO_STATUS_*).
+ * workspace  device, at least fo_workspace_bytes(plan, slots, max_cells).
+ * slots      groups integrated concurrently: 0 launches one block per group;
+ *            a positive value launches that many persistent blocks that pull
+ *            groups from a device queue.
+ * trace      device or NULL: per group, trace_cap records of 4 doubles
+ *            (t, H, err, outcome: 1 accepted, 0 rejected, -1 failed);
+ *            trace_len (device, ngroups int32) receives the record count.
+ */
+int fo_solve(const fo_plan* plan, const fo_options* opt,
+             int32_t ngroups, const int32_t* group_offsets, int32_t max_group_cells,
+             double* Y, int64_t y_cell_stride, int64_t y_species_stride,
+             const double* k, int64_t k_cell_stride, int64_t k_reaction_stride,
+             const double* atol, double rtol, double dt,
+             double* memory, int64_t* counts, int32_t* status,
+             void* workspace, size_t workspace_bytes, int32_t slots,
+             double* trace, int32_t trace_cap, int32_t* trace_len,
+             void* stream);
+
+/* Forcing F(Y) (C x n, written with the Y strides into F) for C cells:
+ * fastode.chem.Mechanism.rhs (fastode/chem.py:89-90). Device pointers. */
+int fo_eval_rhs(const fo_plan* plan, int32_t C,
+                const double* Y, int64_t y_cell_stride, int64_t y_species_stride,
+                const double* k, int64_t k_cell_stride, int64_t k_reaction_stride,
+                double* F, void* stream);
+
+/* Jacobian values on the mechanism's pattern, C x nnz row-major:
+ * fastode.chem.Mechanism.jac_values (fastode/chem.py:92-102). Device pointers. */
+int fo_eval_jac(const fo_plan* plan, int32_t C,
+                const double* Y, int64_t y_cell_stride, int64_t y_species_stride,
+                const double* k, int64_t k_cell_stride, int64_t k_reaction_stride,
+                double* J, void* stream);
+
+/* Last CUDA error text seen by the library (thread-local, never NULL). */
+const char* fo_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTODE_GB300_H */

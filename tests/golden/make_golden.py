@@ -1,0 +1,131 @@
+"""Generate the golden fixtures by running the reference package itself.
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+Imports fastode from the reference checkout (it runs unmodified on NumPy and
+SciPy), integrates the seeded synthetic workloads with
+``fastode.Algorithm(ROS3)`` in a ``run_scenario``-style loop (a fresh Memory per
+group of 32 cells, fastode/ts1.py:196-222), and stores the inputs together with
+the reference's outputs, so that the fixtures are self-contained: tests rebuild
+the mechanism from the stored reaction tables rather than from the generator.
+
+Outputs per case (``<case>.npz``): reactant/product tables, A, E, J, cell
+parameters, Y0, per-interval rate constants, final states, Counts per group,
+status codes per group and interval, final Memory per group, and the
+(t, H, err, outcome) trace of every attempt, recorded by wrapping
+``fastode.solvers.error_norm`` the way experiments/ts1_rejections.py:26-47 does.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+STATUS = {"converged": 0, "too many steps": 1, "step too small": 2, "nan or inf": 3, "projection failed": 4}
+
+
+def reaction_tables(sm):
+    """(reactants, products, yields) as int/float arrays; -1 pads, -2 is M."""
+    R = len(sm.reactions)
+    index = {s: i for i, s in enumerate(sm.species)}
+    rt = np.full((R, 3), -1, dtype=np.int32)
+    pt = np.full((R, 3), -1, dtype=np.int32)
+    yt = np.zeros((R, 3))
+    for j, (reactants, products) in enumerate(sm.reactions):
+        for a, s in enumerate(reactants):
+            rt[j, a] = -2 if s == "M" else index[s]
+        for a, (s, y) in enumerate(products):
+            pt[j, a] = index[s]
+            yt[j, a] = y
+    return rt, pt, yt
+
+
+def run_reference(fastode_mod, wl, n_groups, intervals):
+    from fastode import Algorithm, Counts, ROS3
+    from fastode.chem import ChemSystem, Mechanism
+    import fastode.solvers as S
+
+    rm = Mechanism(wl.sm.species, wl.sm.reactions)
+    C = n_groups * wl.group_size
+    Y0 = wl.cells.Y0[:C]
+    ks = np.stack([wl.k_at(i)[:C] for i in range(intervals)])
+    Y = Y0.copy()
+    counts = np.zeros((n_groups, 13), dtype=np.int64)
+    status = np.zeros((n_groups, intervals), dtype=np.int32)
+    memory = np.zeros((n_groups, 3))
+    traces = []
+    original = S.error_norm
+    original_stages = S.stages
+    for g in range(n_groups):
+        sl = slice(g * wl.group_size, (g + 1) * wl.group_size)
+        alg = Algorithm(ROS3)
+        mem = alg.new_memory()
+        c = Counts()
+        rec = []
+        hrec = []
+
+        def traced(Yv, Ynew, E, atol, rtol, _rec=rec):
+            err = original(Yv, Ynew, E, atol, rtol)
+            _rec.append(err)
+            return err
+
+        def traced_stages(system, tab, Yv, F0, LU, H, cnt, _h=hrec):
+            _h.append(H)
+            return original_stages(system, tab, Yv, F0, LU, H, cnt)
+
+        S.error_norm = traced
+        S.stages = traced_stages
+        try:
+            Yg = Y[sl].copy()
+            for i in range(intervals):
+                Yg, st = alg.solve(ChemSystem(rm, ks[i][sl]), Yg, wl.dt, wl.atol, wl.rtol, c, mem)
+                status[g, i] = STATUS[st]
+        finally:
+            S.error_norm = original
+            S.stages = original_stages
+        Y[sl] = Yg
+        counts[g] = list(c.as_dict().values())
+        memory[g] = (mem.h_next, mem.err_prev, mem.h_prev)
+        traces.append((np.array(hrec), np.array(rec)))
+    L = max(len(t[1]) for t in traces)
+    errs = np.full((n_groups, L), np.nan)
+    hs = np.full((n_groups, L), np.nan)
+    for g, (h, e) in enumerate(traces):
+        errs[g, : len(e)] = e
+        hs[g, : len(h)] = h
+    return dict(Y0=Y0, k=ks, Y=Y, counts=counts, status=status, memory=memory, errs=errs, hs=hs,
+                n_attempts=np.array([len(t[1]) for t in traces]))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    a = ap.parse_args()
+    sys.path.insert(0, a.reference)
+    sys.path.insert(0, str(ROOT))
+    import fastode
+    from fastode_gb300 import synthetic as syn
+
+    cases = {
+        # name: (workload, groups, intervals)
+        "ros3_20x40": (syn.plain_small(), 2, 20),
+        "ros3_210x500": (syn.plain_large(n_cells=64, intervals=4), 2, 4),
+    }
+    for name, (wl, groups, intervals) in cases.items():
+        out = run_reference(fastode, wl, groups, intervals)
+        rt, pt, yt = reaction_tables(wl.sm)
+        np.savez_compressed(
+            HERE / f"{name}.npz",
+            n=wl.sm.n, reactants=rt, products=pt, yields=yt, A=wl.sm.A, E=wl.sm.E, J=wl.sm.J,
+            photolytic=wl.sm.photolytic, T=wl.cells.T[: groups * wl.group_size],
+            p=wl.cells.p[: groups * wl.group_size], phase=wl.cells.phase[: groups * wl.group_size],
+            dt=wl.dt, intervals=intervals, rtol=wl.rtol, atol=wl.atol, group_size=wl.group_size, **out)
+        print(name, "counts", out["counts"].sum(axis=0).tolist())
+
+
+if __name__ == "__main__":
+    main()

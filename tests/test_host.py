@@ -1,0 +1,155 @@
+"""Host-side checks (CPU only): tableaus, mechanism tables, the synthetic
+generator, the C-ABI library's exports and its symbolic analysis."""
+import ctypes
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from golden_cases import CASES, load, mechanism_of, reactions_of
+
+ROOT = Path(__file__).resolve().parents[1]
+REFERENCE = Path("/root/reference")
+
+
+@pytest.mark.parametrize("name", ["ros3", "rodas3"])
+def test_order_conditions(name):
+    # tests/test_fastode.py:21-31
+    from fastode_gb300.tableaus import TABLEAUS
+    tab = TABLEAUS[name]
+    A, Gamma, b, bhat = tab.standard_form()
+    beta = A + Gamma
+    ap = A.sum(axis=1)
+    bp = beta.sum(axis=1)
+    assert abs(b.sum() - 1) < 1e-12
+    assert abs(b @ bp - 0.5) < 1e-12
+    assert abs(b @ ap ** 2 - 1 / 3) < 1e-12
+    assert abs(b @ (beta @ bp) - 1 / 6) < 1e-12
+    assert abs(bhat.sum() - 1) < 1e-12 and abs(bhat @ bp - 0.5) < 1e-12
+
+
+def test_forcing_reuse_flags():
+    # tests/test_fastode.py:39-41
+    from fastode_gb300 import ROS3, RODAS3
+    assert ROS3.new_forcing == [True, True, False]
+    assert RODAS3.new_forcing == [True, False, True, True]
+
+
+def test_quantize():
+    # tests/test_fastode.py:89-93
+    from fastode_gb300 import quantize
+    for h in (1.0, 7.3, 33.0, 600.0, 900.0):
+        q = quantize(h, 600.0)
+        n = round(600.0 / q)
+        assert abs(n * q - 600.0) < 1e-9 and h / 2 < q <= h or h >= 600.0
+
+
+def test_counts_fields_match_device_order():
+    from fastode_gb300.counts import COUNT_FIELDS, Counts
+    c = Counts()
+    assert tuple(c.as_dict().keys()) == COUNT_FIELDS
+    c.add_row(range(13))
+    assert c.calls == 12 and c.steps == 0
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_generator_reproduces_fixture_inputs(case):
+    """The seeded generator still yields the inputs the fixtures were made from."""
+    from fastode_gb300 import synthetic as syn
+    f = load(case)
+    wl = syn.plain_small() if case == "ros3_20x40" else syn.plain_large(n_cells=64, intervals=4)
+    species, reactions = reactions_of(f)
+    assert reactions == wl.sm.reactions
+    C = f["Y0"].shape[0]
+    np.testing.assert_array_equal(wl.cells.Y0[:C], f["Y0"])
+    for i in range(int(f["intervals"])):
+        np.testing.assert_allclose(wl.k_at(i)[:C], f["k"][i], rtol=1e-15, atol=0)
+
+
+@pytest.mark.skipif(not REFERENCE.exists(), reason="reference checkout not present")
+@pytest.mark.parametrize("case", CASES)
+def test_mechanism_tables_match_reference(case):
+    """Mechanism builds the reference's react, S, pattern and GT map."""
+    sys.path.insert(0, str(REFERENCE))
+    from fastode.chem import Mechanism as RMech
+    f = load(case)
+    species, reactions = reactions_of(f)
+    ours = mechanism_of(f)
+    ref = RMech(species, reactions)
+    assert np.array_equal(ours.react, ref.react)
+    assert np.array_equal(ours.S, ref.S)
+    assert np.array_equal(ours.pattern.rows, ref.pattern.rows)
+    assert np.array_equal(ours.pattern.cols, ref.pattern.cols)
+    ind, idx, val = ours.jac_csr()
+    assert np.array_equal(ind, ref.GT.indptr) and np.array_equal(idx, ref.GT.indices)
+    assert np.array_equal(val, ref.GT.data)
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "fastode_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fo_[a-z_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(built_library):
+    lib = ctypes.CDLL(str(built_library))
+    names = declared_symbols()
+    assert "fo_solve" in names and "fo_analyze" in names
+    for name in names:
+        assert hasattr(lib, name), name
+    from fastode_gb300 import _abi
+    assert set(_abi.SIGNATURES) == set(names)
+
+
+def structural_lu(n, rows, cols, perm):
+    """Fill pattern and multiply-add count of a pivot-free dense elimination
+    in the order perm, computed on booleans."""
+    pos = np.empty(n, dtype=np.int64)
+    pos[perm] = np.arange(n)
+    A = np.zeros((n, n), dtype=bool)
+    A[pos[rows], pos[cols]] = True
+    A[np.arange(n), np.arange(n)] = True
+    fma = 0
+    for k in range(n):
+        below = np.nonzero(A[k + 1:, k])[0] + k + 1
+        right = np.nonzero(A[k, k + 1:])[0] + k + 1
+        fma += len(below) * len(right)
+        A[np.ix_(below, right)] = True
+    return A, fma
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("ordering", ["natural", "min_degree", "min_fill", "auto"])
+def test_symbolic_analysis_matches_dense_elimination(built_library, case, ordering):
+    from fastode_gb300.plan import analyze
+    mech = mechanism_of(load(case))
+    info = analyze(mech, ordering)
+    perm = info["perm"]
+    assert sorted(perm.tolist()) == list(range(mech.n))
+    A, fma = structural_lu(mech.n, mech.pattern.rows, mech.pattern.cols, perm)
+    assert info["nnz_lu"] == int(A.sum())
+    assert info["lu_fma"] == fma
+    assert info["nnz_l"] == int(np.tril(A, -1).sum()) and info["nnz_u"] == int(np.triu(A, 1).sum())
+
+
+def test_auto_ordering_is_the_cheapest(built_library):
+    from fastode_gb300.plan import analyze
+    mech = mechanism_of(load("ros3_210x500"))
+    costs = {o: analyze(mech, o)["lu_fma"] for o in ("natural", "min_degree", "min_fill")}
+    assert analyze(mech, "auto")["lu_fma"] <= min(costs.values())
+    assert costs["min_degree"] < costs["natural"]
+
+
+def test_analysis_rejects_bad_descriptors(built_library):
+    from fastode_gb300 import _abi
+    from fastode_gb300.chem import Mechanism
+    from fastode_gb300.plan import _Desc
+    mech = Mechanism(["A", "B"], [(["A"], [("B", 1.0)])])
+    d = _Desc(mech)
+    d.arrays["rows"][0] = 7              # out of range
+    info = _abi.PlanInfo()
+    rc = _abi.lib().fo_analyze(ctypes.byref(d.desc), 0, ctypes.byref(info), None)
+    assert rc == -1
+    assert b"out of range" in _abi.lib().fo_last_error()

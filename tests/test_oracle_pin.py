@@ -1,0 +1,149 @@
+"""Pin the oracle to the reference: the golden fixtures hold the reference's own
+outputs (tests/golden/make_golden.py), and the controller cases restate the
+known answers of the reference's unit tests (tests/test_fastode.py:89-208) on
+one-species mechanisms. CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+from golden_cases import CASES, load, mechanism_of
+from oracle import rosenbrock as O
+
+STATUS = ("converged", "too many steps", "step too small", "nan or inf", "projection failed")
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_reproduces_reference_fixture(case):
+    f = load(case)
+    mech = mechanism_of(f)
+    G = f["counts"].shape[0]
+    gs = int(f["group_size"])
+    intervals = int(f["intervals"])
+    ks = f["k"]
+    Y, counts, statuses, mems, traces = O.run_groups(
+        mech, f["Y0"], lambda i: ks[i], float(f["dt"]), intervals, f["atol"], float(f["rtol"]),
+        group_size=gs, trace=True)
+    # the same NumPy/SciPy operations on the same inputs: bit-identical
+    np.testing.assert_array_equal(Y, f["Y"])
+    for g in range(G):
+        assert counts[g].as_tuple() == tuple(f["counts"][g])
+        assert [STATUS.index(s) for s in statuses[g]] == list(f["status"][g])
+        assert (mems[g].h_next, mems[g].err_prev, mems[g].h_prev) == tuple(f["memory"][g])
+        na = int(f["n_attempts"][g])
+        assert [t[2] for t in traces[g]] == list(f["errs"][g, :na])
+        assert [t[1] for t in traces[g]] == list(f["hs"][g, :na])
+
+
+def one_species(lam):
+    """y' = -lam*y as the mechanism A -> (nothing) with k = lam."""
+    from fastode_gb300.chem import Mechanism
+    return Mechanism(["A"], [(["A"], [])]), np.array([[lam]])
+
+
+def test_oracle_quantize():
+    # tests/test_fastode.py:89-93
+    for h in (1.0, 7.3, 33.0, 600.0, 900.0):
+        q = O.quantize(h, 600.0)
+        n = round(600.0 / q)
+        assert abs(n * q - 600.0) < 1e-9 and h / 2 < q <= h or h >= 600.0
+
+
+def test_oracle_carried_step_takes_one_step():
+    # tests/test_fastode.py:96-110
+    mech, k = one_species(1e-6)
+    alg = O.OAlgorithm(O.OROS3)
+    mem = O.OMemory()
+    Y = np.array([[1.0]])
+    c = O.OCounts()
+    for _ in range(5):
+        Y, _ = alg.solve(O.OChem(mech, k), Y, 600.0, np.array([1e-10]), 1e-3, c, mem)
+    c3 = O.OCounts()
+    alg.solve(O.OChem(mech, k), Y, 600.0, np.array([1e-10]), 1e-3, c3, mem)
+    assert c3.accepted == 1
+
+
+def test_oracle_quantized_steps_land_on_interval_end():
+    # tests/test_fastode.py:113-125
+    mech, k = one_species(1e-9)
+    alg = O.OAlgorithm(O.OROS3, fac_max=1.0)
+    mem = O.OMemory(h_next=600.0 / 7)
+    Y = np.array([[1.0]])
+    for _ in range(3):
+        c = O.OCounts()
+        Y, st = alg.solve(O.OChem(mech, k), Y, 600.0, np.array([1e-10]), 1e-3, c, mem)
+        assert st == "converged" and c.steps == 7
+        assert abs(mem.h_next - 600.0 / 7) < 1e-9
+
+
+def test_oracle_rejection_shrinks_step():
+    # tests/test_fastode.py:128-136
+    mech, k = one_species(1.0)
+    alg = O.OAlgorithm(O.OROS3)
+    mem = O.OMemory(1.0, 1e-8, 1.0)
+    c = O.OCounts()
+    alg.solve(O.OChem(mech, k), np.array([[1.0]]), 1.0, np.array([1e-12]), 4e-3, c, mem)
+    assert c.rejected == 1
+
+
+def test_oracle_no_forced_acceptance_below_minimum_step():
+    # tests/test_fastode.py:152-169
+    mech, k = one_species(1e15)
+    alg = O.OAlgorithm(O.OROS3, max_steps=10)
+    mem = O.OMemory(h_next=1e-15)
+    c = O.OCounts()
+    y0 = np.array([[1.0]])
+    y, st = alg.solve(O.OChem(mech, k), y0, 1.0, np.array([1e-30]), 1e-12, c, mem)
+    assert st == "step too small"
+    assert c.steps == c.rejected == 1 and c.accepted == 0
+    np.testing.assert_array_equal(y, y0)
+
+
+@pytest.mark.parametrize("budget", [0, 1, 2])
+def test_oracle_budget_includes_rejected(budget):
+    # tests/test_fastode.py:172-187
+    mech, k = one_species(1.0)
+    alg = O.OAlgorithm(O.OROS3, max_steps=budget)
+    mem = O.OMemory(h_next=1.0)
+    c = O.OCounts()
+    y0 = np.array([[1.0]])
+    y, st = alg.solve(O.OChem(mech, k), y0, 1.0, np.array([1e-30]), 1e-13, c, mem)
+    assert st == "too many steps"
+    assert c.steps == c.rejected == budget and c.accepted == 0
+    np.testing.assert_array_equal(y, y0)
+
+
+@pytest.mark.parametrize("budget, expected", [(2, "too many steps"), (10, "converged")])
+def test_oracle_budget_includes_accepted(budget, expected):
+    # tests/test_fastode.py:190-208
+    mech, k = one_species(1e-6)
+    alg = O.OAlgorithm(O.OROS3, max_steps=budget, fac_max=1.0)
+    mem = O.OMemory(h_next=0.1)
+    c = O.OCounts()
+    _, st = alg.solve(O.OChem(mech, k), np.array([[1.0]]), 1.0, np.array([1e-10]), 1e-3, c, mem)
+    assert st == expected
+    assert c.steps == c.accepted == budget and c.rejected == 0
+
+
+def test_oracle_linear_invariant():
+    # tests/test_fastode.py:68-72: Robertson conserves A + B + C under fixed steps
+    from fastode_gb300.chem import Mechanism
+    mech = Mechanism(["A", "B", "C"], [(["A"], [("B", 1.0)]), (["B", "B"], [("B", 1.0), ("C", 1.0)]),
+                                       (["B", "C"], [("A", 1.0), ("C", 1.0)])])
+    k = np.array([[0.04, 3.0e7, 1.0e4]])
+    for tab in (O.OROS3, O.ORODAS3):
+        Y = O.fixed_steps(O.OChem(mech, k), tab, np.array([[1.0, 0.0, 0.0]]), 1.0e-2, 50)
+        assert abs(Y.sum() - 1.0) < 1e-14
+
+
+def test_oracle_order_three():
+    # tests/test_fastode.py:44-51 restated on a mass-action mechanism:
+    # A + A + A -> 2A gives y' = -y^3 with k = 1
+    from fastode_gb300.chem import Mechanism
+    mech = Mechanism(["A"], [(["A", "A", "A"], [("A", 2.0)])])
+    exact = 1.0 / math.sqrt(3.0)
+    for tab in (O.OROS3, O.ORODAS3):
+        errs = [abs(O.fixed_steps(O.OChem(mech, np.array([[1.0]])), tab, np.array([[1.0]]), 1.0, n)[0, 0] - exact)
+                for n in (20, 40, 80)]
+        orders = [math.log2(errs[i] / errs[i + 1]) for i in range(2)]
+        assert min(orders) > 2.8
