@@ -1,0 +1,330 @@
+"""Throughput of the GB300 Rosenbrock integrator: cell-intervals per second.
+
+Workload (one "step" = one host interval over every cell): the plain ROS3 drop-in
+configuration — a seeded synthetic mass-action mechanism of 210 species and 500
+reactions, 65,536 cells in groups of 32, T U[200, 310] K, p U[10, 1000] hPa
+setting [M], dt = 30 s, rtol 1e-3, atol = rtol * 1e-14, photolysis updated at
+every interval start. FP64 throughout. The timed job starts from the initial
+state (the cold first interval included) and runs K intervals.
+
+    python bench.py [--steps K] [--warmup W] [--cells C] [--impl ours|reference]
+
+Prints one JSON line. ``value`` is device-resident throughput (state, rate
+constants and controller memory in HBM; per interval one photolysis-update
+kernel and one integrator launch); ``e2e`` is the same metric through the
+public host API (host arrays in, host arrays out, copies timed); ``roofline``
+relates the integrator kernel's algorithmic FP64 rate to the FP64 FMA rate
+measured on the same GPU in the same run; ``cpu_baseline`` is the oracle (a
+NumPy/SciPy restatement of the reference) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-intervals/s at rtol=1e-3 on 1 GB300 vs plain GPU + CPU ref; adjoint/forward cost"
+
+
+# ---- CPU baseline: the oracle in a spawn pool, one group per worker --------------------
+
+def _cpu_worker(args):
+    """Integrate one group of the workload over `intervals` intervals with the
+    oracle; returns (cells, intervals, seconds)."""
+    group, n_cells, intervals = args
+    os.environ["OMP_NUM_THREADS"] = os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, str(ROOT))
+    from fastode_gb300 import synthetic as syn
+    from oracle import rosenbrock as O
+    wl = syn.plain_large(n_cells=n_cells, intervals=intervals).subset(slice(group * 32, group * 32 + 32))
+    t0 = time.perf_counter()
+    O.run_groups(wl.sm.mech, wl.cells.Y0, wl.k_at, wl.dt, intervals, wl.atol, wl.rtol)
+    return 32, intervals, time.perf_counter() - t0
+
+
+def cpu_baseline(n_cells, intervals, workers):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    groups = list(range(workers))
+    t0 = time.perf_counter()
+    with ctx.Pool(workers) as pool:
+        res = pool.map(_cpu_worker, [(g, n_cells, intervals) for g in groups])
+    wall = time.perf_counter() - t0
+    cell_int = sum(c * i for c, i, _ in res)
+    per_core = statistics.mean(c * i / s for c, i, s in res)
+    return cell_int / wall, per_core, wall
+
+
+# ---- clocks during the timed region ----------------------------------------------------
+
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---- the GPU arm ---------------------------------------------------------------------
+
+def algorithmic_flops(plan, counts_rows, offsets):
+    """FP64 operations the algorithm needs for these Counts rows (per group:
+    lu, solves, rhs, jac, steps) times the cells of each group."""
+    f = plan.flops_per_attempt()
+    n = plan.n
+    cells = np.diff(offsets).astype(np.float64)
+    c = counts_rows.astype(np.float64)
+    steps, lu, solves, rhs, jac = c[:, 0], c[:, 5], c[:, 6], c[:, 3], c[:, 4]
+    # per attempt besides LU and solves: stage combinations and the error norm
+    per_step = 14 * n
+    per_group = lu * f["lu"] + solves * f["solve"] + rhs * f["rhs"] + jac * f["jac"] + steps * per_step
+    return float((per_group * cells).sum())
+
+
+def run_ours(args, rank, world):
+    import ctypes as C
+    import torch
+    from fastode_gb300 import _abi, build as fbuild, synthetic as syn
+    from fastode_gb300.batch import Batch, solve_host
+
+    fbuild.build()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    lib = _abi.lib()
+    fma_rate = C.c_double()
+    _abi.check(lib.fo_fp64_fma_rate(C.byref(fma_rate)), "fo_fp64_fma_rate")
+
+    wl = syn.plain_large(n_cells=args.cells, intervals=args.steps)
+    sm, cells = wl.sm, wl.cells
+    Cc, R, n = cells.C, sm.R, sm.n
+    M = cells.p / (syn.R_GAS * cells.T)
+    photo = np.nonzero(sm.photolytic)[0].astype(np.int32)
+    d = {name: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for name, v in
+         dict(A=sm.A, E=sm.E, power=sm.mech.third_body_power, T=cells.T, M=M, phase=cells.phase,
+              J=sm.J[photo], rxn=photo, atol=wl.atol).items()}
+    k = torch.empty((R, Cc), dtype=torch.float64, device=dev)          # cells fastest
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    omega = 2.0 * np.pi / 86400.0
+
+    def thermal():
+        _abi.check(lib.fo_rate_constants(Cc, R, d["A"].data_ptr(), d["E"].data_ptr(), d["power"].data_ptr(),
+                                         d["T"].data_ptr(), d["M"].data_ptr(), k.data_ptr(), 1, Cc, sp),
+                   "fo_rate_constants")
+
+    def photolysis(i):
+        _abi.check(lib.fo_update_photolysis(Cc, len(photo), d["rxn"].data_ptr(), d["J"].data_ptr(),
+                                            d["phase"].data_ptr(), omega, i * wl.dt, k.data_ptr(), 1, Cc, sp),
+                   "fo_update_photolysis")
+
+    thermal()
+    Y0 = torch.from_numpy(cells.Y0).to(dev)
+    batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots)
+
+    def reset():
+        batch.Y.copy_(Y0.t())
+        batch.memory.zero_()
+        batch.counts.zero_()
+        batch.status.zero_()
+
+    for i in range(args.warmup):                     # untimed: the same kernels and shapes
+        photolysis(i)
+        batch.step(k, wl.dt, d["atol"], wl.rtol)
+    torch.cuda.synchronize()
+    reset()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev.index) as clocks:
+        start.record()
+        for i in range(args.steps):
+            photolysis(i)
+            ev[i][0].record()
+            batch.step(k, wl.dt, d["atol"], wl.rtol)
+            ev[i][1].record()
+        end.record()
+        torch.cuda.synchronize()
+    elapsed = start.elapsed_time(end) / 1e3
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    solve_ms = [a.elapsed_time(b) for a, b in ev]
+    counts = batch.counts.cpu().numpy()
+    statuses = batch.statuses()
+    flops = algorithmic_flops(batch.plan, counts, batch.offsets_host)
+    kernel_s = sum(solve_ms) / 1e3
+    achieved = flops / kernel_s / 1e12
+    peak = 2.0 * fma_rate.value / 1e12
+    value = Cc * args.steps * world / elapsed
+
+    # e2e through the public host API: host arrays in and out, copies timed
+    e2e_steps = min(args.steps, args.e2e_steps)
+    e2e = None
+    if e2e_steps > 0:
+        pinned_k = [torch.from_numpy(wl.k_at(i)).pin_memory() for i in range(e2e_steps)]
+        Yh = torch.from_numpy(cells.Y0.copy()).pin_memory()
+        state = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h2d = d2h = 0
+        for i in range(e2e_steps):
+            Yh, state, moved = solve_host(sm.mech, Yh, pinned_k[i], wl.dt, wl.atol, wl.rtol, state=state,
+                                          group_size=32, slots=args.slots)
+            h2d += moved[0]
+            d2h += moved[1]
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": Cc * e2e_steps / e2e_s, "unit": "cell-intervals/s", "steps": e2e_steps,
+               "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
+               "api": "fastode_gb300.batch.solve_host (host (C,n) state and (C,R) rate constants)"}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "cell-intervals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": {"workload": "ros3-210x500: synthetic 210 species / 500 reactions, 65,536 cells in groups "
+                               "of 32, dt=30 s, rtol=1e-3, photolysis per interval" if Cc == 65536 else
+                               f"ros3-210x500 with {Cc} cells",
+                   "cells": Cc, "group_size": 32, "intervals_timed": args.steps, "dt": wl.dt, "rtol": wl.rtol,
+                   "l2": "inputs larger than L2 (state 110 MB + rate constants 262 MB + scratch per interval)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "slots": args.slots or "one block per group"},
+        "gpu_launches": 2 * args.steps,
+        "statuses": {s: statuses.count(s) for s in set(statuses)},
+        "counts_per_group_interval": {
+            "attempts": float(counts[:, 0].sum() / len(counts) / args.steps),
+            "rejected": float(counts[:, 2].sum() / len(counts) / args.steps)},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "solve_kernel", "kernel_ms_per_launch": sum(solve_ms) / len(solve_ms),
+                     "peak_source": "fo_fp64_fma_rate: full-warp DFMA kernel, same GPU, same run (the driver's "
+                                    "peaks file holds HBM and bf16 only)",
+                     "algorithmic_flops_per_launch": flops / args.steps},
+        "clocks": clocks.summary(),
+        "e2e": e2e,
+    }
+    if rank == 0 and args.cpu_intervals > 0 and not args.no_cpu:
+        workers = args.cpu_workers or os.cpu_count()
+        thr, per_core, wall = cpu_baseline(args.cells, args.cpu_intervals, workers)
+        out["cpu_baseline"] = {"value": thr, "unit": "cell-intervals/s", "cores": workers, "kind": "port",
+                               "per_core": per_core,
+                               "sample": f"{workers} groups of 32 cells x the first {args.cpu_intervals} "
+                                         f"intervals (cold start included), one group per process, "
+                                         f"BLAS 1 thread, {wall:.1f} s wall"}
+    return out
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle port: the reference is Python and
+    does not travel) on every host core: each step advances one group per
+    worker by one interval."""
+    import multiprocessing as mp
+    workers = args.cpu_workers or os.cpu_count()
+    ctx = mp.get_context("spawn")
+    from oracle.pool import GroupPool
+    with GroupPool(ctx, workers, args.cells) as pool:
+        for i in range(args.warmup):
+            pool.step()
+        pool.reset()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            pool.step()
+        wall = time.perf_counter() - t0
+    value = workers * 32 * args.steps / wall
+    return {
+        "metric": METRIC, "value": value, "unit": "cell-intervals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": {"workload": "ros3-210x500 (sample)", "cells": args.cells, "group_size": 32},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "cell-intervals/s", "cores": workers, "kind": "port",
+                         "sample": f"{workers} groups of 32 cells (one per process), each step one interval "
+                                   f"of each, from the initial state"},
+        "e2e": {"value": value, "unit": "cell-intervals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=120)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--cells", type=int, default=65536)
+    ap.add_argument("--slots", type=int, default=0)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--cpu-intervals", type=int, default=30)
+    ap.add_argument("--cpu-workers", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args, rank, world)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -46,7 +46,10 @@ class Options(C.Structure):
     _fields_ = [("tableau", C.c_int32), ("controller", C.c_int32), ("b", C.c_double),
                 ("safety", C.c_double), ("fac_min", C.c_double), ("fac_max", C.c_double),
                 ("carry", C.c_int32), ("quantize", C.c_int32), ("carry_memory", C.c_int32),
-                ("max_steps", C.c_int32)]
+                ("max_steps", C.c_int32), ("variant", C.c_int32)]
+
+
+VARIANTS = {"pipelined": 0, "plain": 1}
 
 
 _P = C.c_void_p
@@ -68,6 +71,9 @@ SIGNATURES = {
                            _P, _P, _P, _P, C.c_size_t, _I32, _P, _I32, _P, _P]),
     "fo_eval_rhs": (C.c_int, [_P, _I32, _P, _I64, _I64, _P, _I64, _I64, _P, _P]),
     "fo_eval_jac": (C.c_int, [_P, _I32, _P, _I64, _I64, _P, _I64, _I64, _P, _P]),
+    "fo_rate_constants": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
+    "fo_update_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _D, _P, _I64, _I64, _P]),
+    "fo_fp64_fma_rate": (C.c_int, [C.POINTER(C.c_double)]),
 }
 
 _lib = None

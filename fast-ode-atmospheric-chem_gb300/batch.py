@@ -89,3 +89,68 @@ class Batch:
 
     def statuses(self) -> list:
         return [_abi.STATUS_STRINGS[int(s)] for s in self.status.cpu().numpy()]
+
+
+class HostState:
+    """Device buffers and per-group controller memory carried between
+    ``solve_host`` calls (the reference's per-group Memory of
+    fastode/ts1.py:201, kept on the device)."""
+
+    def __init__(self, mech, C_cells, n, R, group_size, algorithm, mass, slots, dev):
+        import torch
+        self.alg = algorithm if algorithm is not None else Algorithm()
+        self.plan = plan_for(mech, mass, self.alg.ordering)
+        offs = group_offsets(C_cells, group_size)
+        self.ngroups = len(offs) - 1
+        self.max_cells = int(np.max(np.diff(offs)))
+        self.offsets = torch.from_numpy(offs).to(dev)
+        self.Y = torch.empty((C_cells, n), dtype=torch.float64, device=dev)
+        self.k = torch.empty((C_cells, R), dtype=torch.float64, device=dev)
+        self.atol = torch.empty(n, dtype=torch.float64, device=dev)
+        self.memory = torch.zeros((self.ngroups, 3), dtype=torch.float64, device=dev)
+        self.counts = torch.zeros((self.ngroups, len(COUNT_FIELDS)), dtype=torch.int64, device=dev)
+        self.status = torch.zeros(self.ngroups, dtype=torch.int32, device=dev)
+        self.slots = int(slots)
+        grid = self.ngroups if self.slots <= 0 else min(self.slots, self.ngroups)
+        self.ws = torch.empty(self.plan.workspace_bytes(grid, self.max_cells), dtype=torch.uint8, device=dev)
+        self.Y_out = torch.empty((C_cells, n), dtype=torch.float64).pin_memory()
+        self.status_out = torch.empty(self.ngroups, dtype=torch.int32).pin_memory()
+        self.opts = self.alg.options()
+        self.shape = (C_cells, n, R)
+
+
+def solve_host(mech, Y, k, dt, atol, rtol, state: HostState = None, group_size: int = 32,
+               algorithm: Algorithm = None, mass=None, slots: int = 0):
+    """Integrate the cells of host arrays Y (C, n) and k (C, R), both in the
+    reference's cell-major layout, over one interval, in groups of
+    `group_size` cells that each carry their own controller memory from call
+    to call in `state`. Returns (Y_new (C, n) host tensor, state,
+    (bytes host-to-device, bytes device-to-host)). Pinned host tensors copy
+    fastest. The statuses of the call are in ``state.status_out``."""
+    import torch
+    Yt = Y if isinstance(Y, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(Y, dtype=np.float64))
+    kt = k if isinstance(k, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(k, dtype=np.float64))
+    C_cells, n = Yt.shape
+    R = kt.shape[1]
+    if state is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+        state = HostState(mech, C_cells, n, R, group_size, algorithm, mass, slots, dev)
+    if state.shape != (C_cells, n, R):
+        raise ValueError("state was made for other shapes")
+    s = torch.cuda.current_stream(state.Y.device)
+    state.Y.copy_(Yt, non_blocking=True)
+    state.k.copy_(kt, non_blocking=True)
+    at = torch.from_numpy(np.array(np.broadcast_to(np.asarray(atol, dtype=np.float64), (n,))))
+    state.atol.copy_(at, non_blocking=False)
+    rc = _abi.lib().fo_solve(
+        state.plan.handle, C.byref(state.opts), state.ngroups, state.offsets.data_ptr(), state.max_cells,
+        state.Y.data_ptr(), n, 1, state.k.data_ptr(), R, 1, state.atol.data_ptr(), float(rtol), float(dt),
+        state.memory.data_ptr(), state.counts.data_ptr(), state.status.data_ptr(),
+        state.ws.data_ptr(), state.ws.numel(), state.slots, None, 0, None, C.c_void_p(s.cuda_stream))
+    _abi.check(rc, "fo_solve")
+    state.Y_out.copy_(state.Y, non_blocking=True)
+    state.status_out.copy_(state.status, non_blocking=True)
+    s.synchronize()
+    h2d = Yt.numel() * 8 + kt.numel() * 8 + n * 8
+    d2h = state.Y_out.numel() * 8 + state.status_out.numel() * 4
+    return state.Y_out, state, (h2d, d2h)

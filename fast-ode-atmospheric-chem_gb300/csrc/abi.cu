@@ -160,7 +160,8 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
          o_sptr = append(buf, t.s_ptr), o_srxn = append(buf, t.s_rxn), o_sval = append(buf, t.s_val),
          o_jrow = append(buf, t.j_row_ptr), o_jcol = append(buf, t.j_col), o_jsrc = append(buf, t.j_src),
          o_jtp = append(buf, t.jt_ptr), o_jti = append(buf, t.jt_idx), o_jtv = append(buf, t.jt_val),
-         o_lur = append(buf, t.lu_row_ptr), o_lud = append(buf, t.lu_diag), o_luc = append(buf, t.lu_col);
+         o_lur = append(buf, t.lu_row_ptr), o_lud = append(buf, t.lu_diag), o_luc = append(buf, t.lu_col),
+         o_elp = append(buf, t.el_ptr), o_el = append(buf, t.el);
   cudaError_t e = cudaGetDevice(&plan->device);
   if (e != cudaSuccess) {
     delete plan;
@@ -199,6 +200,8 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
   d.lu_row_ptr = reinterpret_cast<const int32_t*>(b + o_lur);
   d.lu_diag = reinterpret_cast<const int32_t*>(b + o_lud);
   d.lu_col = reinterpret_cast<const int32_t*>(b + o_luc);
+  d.el_ptr = reinterpret_cast<const int32_t*>(b + o_elp);
+  d.el = reinterpret_cast<const int2*>(b + o_el);
   d.has_constraints = 0;
   for (double m : t.mass)
     if (m == 0.0) d.has_constraints = 1;
@@ -244,7 +247,6 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
     return fail(FO_E_INVALID, "unknown tableau");
   if (max_group_cells <= 0 || max_group_cells > kMaxLanes)
     return fail(FO_E_UNSUPPORTED, "group size must be 1..256 cells");
-  if (plan->dev.has_constraints) return fail(FO_E_UNSUPPORTED, "constrained (mass = 0) species need the projection");
   if (!(dt > 0.0)) return fail(FO_E_INVALID, "dt must be positive");
   if (opt->max_steps < 0) return fail(FO_E_INVALID, "max_steps must be non-negative");
   const int lanes = lanes_for(max_group_cells);
@@ -272,6 +274,9 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   p.o.quantize = opt->quantize;
   p.o.carry_memory = opt->carry_memory;
   p.o.max_steps = opt->max_steps;
+  p.o.variant = opt->variant;
+  if (opt->variant != FO_VARIANT_PIPELINED && opt->variant != FO_VARIANT_PLAIN)
+    return fail(FO_E_INVALID, "unknown kernel variant");
   p.o.k_exp = 3.0;  // embedded order 2 for both tableaus
   p.ngroups = ngroups;
   p.group_offsets = group_offsets;

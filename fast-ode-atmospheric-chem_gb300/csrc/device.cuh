@@ -23,6 +23,8 @@ struct DevTables {
   const int32_t* lu_row_ptr;  // n+1
   const int32_t* lu_diag;     // n
   const int32_t* lu_col;      // nlu
+  const int32_t* el_ptr;      // n+1: elimination stream rows (entries)
+  const int2* el;             // stream entries (x, y)
   int has_constraints;
 };
 
@@ -38,6 +40,7 @@ struct DevOptions {
   int controller;  // 0 h211b, 1 elementary
   double b, safety, fac_min, fac_max;
   int carry, quantize, carry_memory, max_steps;
+  int variant;     // FO_VARIANT_*
   double k_exp;    // embedded order + 1
 };
 

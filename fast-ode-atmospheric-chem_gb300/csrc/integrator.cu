@@ -22,6 +22,7 @@
 // roundoff; the LU, the triangular solves and the sparse map to Jacobian
 // values use FMA.
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include <cmath>
 #include <cstdint>
@@ -121,13 +122,30 @@ __device__ void eval_negjac(const SolveParams& p, const Lane& ln, const double* 
   }
 }
 
+// Row r of the stage matrix alpha*M - J scattered into the dense work row w
+// over the row's filled pattern (fastode/linalg.py:60-67). With alg_only,
+// the projection's matrix diag(M) - J with the differential rows of J
+// dropped (fastode/linalg.py:62-63, alpha = 1).
+__device__ __forceinline__ void assemble_row(const SolveParams& p, const Lane& ln, int r, int q0, int q1,
+                                             double alpha, const double* negj, double* w, bool alg_only) {
+  const int L = ln.L, lane = ln.lane;
+  const int32_t* __restrict__ col = p.t.lu_col;
+  for (int q = q0; q < q1; ++q) WROW(__ldg(col + q)) = 0.0;
+  const double mr = __ldg(p.t.mass + r);
+  if (!alg_only || mr == 0.0) {
+    const int e1 = __ldg(p.t.j_row_ptr + r + 1);
+    for (int e = __ldg(p.t.j_row_ptr + r); e < e1; ++e) WROW(__ldg(p.t.j_col + e)) = SCR(negj, e);
+  }
+  WROW(r) = __dadd_rn(WROW(r), __dmul_rn(alpha, mr));
+}
+
 // In-place pivot-free LU of alpha*M - J on the precomputed fill pattern,
 // row by row (up-looking). Row r is scattered into the dense work row w,
 // eliminated with the finished rows above it, and gathered back. The
 // diagonal slot keeps the reciprocal of the pivot. Replaces SuperLU's gstrf
 // (fastode/linalg.py:70-78) and LAPACK getrf (fastode/linalg.py:15-18).
-__device__ void factor(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
-                       double* w) {
+__device__ __noinline__ void factor(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
+                       double* w, bool alg_only) {
   const int L = ln.L, lane = ln.lane;
   const int n = p.t.n;
   const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
@@ -135,10 +153,7 @@ __device__ void factor(const SolveParams& p, const Lane& ln, double alpha, const
   const int32_t* __restrict__ col = p.t.lu_col;
   for (int r = 0; r < n; ++r) {
     const int q0 = __ldg(rowp + r), q1 = __ldg(rowp + r + 1), dg = __ldg(diag + r);
-    for (int q = q0; q < q1; ++q) WROW(__ldg(col + q)) = 0.0;
-    const int e1 = __ldg(p.t.j_row_ptr + r + 1);
-    for (int e = __ldg(p.t.j_row_ptr + r); e < e1; ++e) WROW(__ldg(p.t.j_col + e)) = SCR(negj, e);
-    WROW(r) = __dadd_rn(WROW(r), __dmul_rn(alpha, __ldg(p.t.mass + r)));
+    assemble_row(p, ln, r, q0, q1, alpha, negj, w, alg_only);
     for (int q = q0; q < dg; ++q) {
       const int k = __ldg(col + q);
       const double l = WROW(k) * SCR(lu, __ldg(diag + k));
@@ -163,6 +178,134 @@ __device__ void factor(const SolveParams& p, const Lane& ln, double alpha, const
   }
 }
 
+// The same factorization driven by the precomputed elimination stream
+// (symbolic.h): every row's updates and multipliers are one flat sequence of
+// (x, y) entries, processed in chunks of kChunk with the next chunk's loads
+// (U entries of finished rows and pivot reciprocals, which no entry of the
+// row writes) issued before the current chunk computes. The warp keeps
+// kChunk 256-byte loads in flight while its FP64 pipe works.
+constexpr int kChunk = 16;
+
+__device__ __forceinline__ void stream_load(const int2* __restrict__ meta, const double* __restrict__ lu, int L,
+                                            int lane, int2 (&m)[kChunk], double (&v)[kChunk]) {
+#pragma unroll
+  for (int s = 0; s < kChunk; s += 2) {
+    const int4 mm = __ldg(reinterpret_cast<const int4*>(meta + s));
+    m[s] = make_int2(mm.x, mm.y);
+    m[s + 1] = make_int2(mm.z, mm.w);
+  }
+#pragma unroll
+  for (int s = 0; s < kChunk; ++s) {
+    const int x = m[s].x;
+    const int pos = x >= 0 ? x : -1 - x;
+    v[s] = lu[(int64_t)pos * L + lane];
+  }
+}
+
+__device__ __forceinline__ void stream_compute(const int2 (&m)[kChunk], const double (&v)[kChunk], double* w,
+                                               double* lu, int L, int lane, double& l, int& q) {
+#pragma unroll
+  for (int s = 0; s < kChunk; ++s) {
+    const int x = m[s].x, y = m[s].y;
+    if (x >= 0) {
+      WROW(y) = fma(-l, v[s], WROW(y));
+    } else if (y >= 0) {
+      l = WROW(y) * v[s];
+      SCR(lu, q) = l;
+      ++q;
+    }
+  }
+}
+
+__device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
+                              double* w, bool alg_only) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n;
+  const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
+  const int32_t* __restrict__ diag = p.t.lu_diag;
+  const int32_t* __restrict__ col = p.t.lu_col;
+  for (int r = 0; r < n; ++r) {
+    const int q0 = __ldg(rowp + r), q1 = __ldg(rowp + r + 1), dg = __ldg(diag + r);
+    assemble_row(p, ln, r, q0, q1, alpha, negj, w, alg_only);
+    const int t0 = __ldg(p.t.el_ptr + r), t1 = __ldg(p.t.el_ptr + r + 1);
+    double l = 0.0;
+    int q = q0;
+    if (t1 > t0) {
+      int2 mA[kChunk], mB[kChunk];
+      double vA[kChunk], vB[kChunk];
+      stream_load(p.t.el + t0, lu, L, lane, mA, vA);
+      int t = t0;
+      for (;;) {
+        const bool more = t + kChunk < t1;
+        if (more) stream_load(p.t.el + t + kChunk, lu, L, lane, mB, vB);
+        stream_compute(mA, vA, w, lu, L, lane, l, q);
+        t += kChunk;
+        if (!more) break;
+        const bool more2 = t + kChunk < t1;
+        if (more2) stream_load(p.t.el + t + kChunk, lu, L, lane, mA, vA);
+        stream_compute(mB, vB, w, lu, L, lane, l, q);
+        t += kChunk;
+        if (!more2) break;
+      }
+    }
+    SCR(lu, dg) = 1.0 / WROW(r);
+    for (int qq = dg + 1; qq < q1; ++qq) SCR(lu, qq) = WROW(__ldg(col + qq));
+  }
+}
+
+// Forward and backward substitution with the factor entries of a row loaded
+// eight at a time ahead of their use, two partial sums per row.
+__device__ void lu_solve_pipelined(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n;
+  const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
+  const int32_t* __restrict__ diag = p.t.lu_diag;
+  const int32_t* __restrict__ col = p.t.lu_col;
+  for (int r = 0; r < n; ++r) {
+    double a0 = WROW(r), a1 = 0.0;
+    int q = __ldg(rowp + r);
+    const int dg = __ldg(diag + r);
+    for (; q + 7 < dg; q += 8) {
+      double v[8];
+      int c[8];
+#pragma unroll
+      for (int s = 0; s < 8; ++s) {
+        v[s] = SCR(lu, q + s);
+        c[s] = __ldg(col + q + s);
+      }
+#pragma unroll
+      for (int s = 0; s < 8; s += 2) {
+        a0 = fma(-v[s], WROW(c[s]), a0);
+        a1 = fma(-v[s + 1], WROW(c[s + 1]), a1);
+      }
+    }
+    for (; q < dg; ++q) a0 = fma(-SCR(lu, q), WROW(__ldg(col + q)), a0);
+    WROW(r) = a0 + a1;
+  }
+  for (int r = n - 1; r >= 0; --r) {
+    double a0 = WROW(r), a1 = 0.0;
+    const int dg = __ldg(diag + r), q1 = __ldg(rowp + r + 1);
+    const double dinv = SCR(lu, dg);
+    int q = dg + 1;
+    for (; q + 7 < q1; q += 8) {
+      double v[8];
+      int c[8];
+#pragma unroll
+      for (int s = 0; s < 8; ++s) {
+        v[s] = SCR(lu, q + s);
+        c[s] = __ldg(col + q + s);
+      }
+#pragma unroll
+      for (int s = 0; s < 8; s += 2) {
+        a0 = fma(-v[s], WROW(c[s]), a0);
+        a1 = fma(-v[s + 1], WROW(c[s + 1]), a1);
+      }
+    }
+    for (; q < q1; ++q) a0 = fma(-SCR(lu, q), WROW(__ldg(col + q)), a0);
+    WROW(r) = (a0 + a1) * dinv;
+  }
+}
+
 // Forward and backward substitution in place on w (fastode/linalg.py:80-81).
 __device__ void lu_solve(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
   const int L = ln.L, lane = ln.lane;
@@ -182,6 +325,26 @@ __device__ void lu_solve(const SolveParams& p, const Lane& ln, const double* lu,
     for (int q = dg + 1; q < q1; ++q) acc = fma(-SCR(lu, q), WROW(__ldg(col + q)), acc);
     WROW(r) = acc * SCR(lu, dg);
   }
+}
+
+__device__ void factor_any(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
+                           double* w, bool alg_only) {
+  if (p.o.variant == FO_VARIANT_PLAIN) factor(p, ln, alpha, negj, lu, w, alg_only);
+  else factor_stream(p, ln, alpha, negj, lu, w, alg_only);
+}
+
+__device__ __forceinline__ void solve_in_w(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
+  if (p.o.variant == FO_VARIANT_PLAIN) lu_solve(p, ln, lu, w);
+  else lu_solve_pipelined(p, ln, lu, w);
+}
+
+// x = A^-1 b with the factors in lu (b and x per-lane vectors, may alias).
+__device__ void solve_into(const SolveParams& p, const Lane& ln, const double* lu, double* w, const double* b,
+                           double* x) {
+  const int L = ln.L, lane = ln.lane;
+  for (int i = 0; i < p.t.n; ++i) WROW(i) = SCR(b, i);
+  solve_in_w(p, ln, lu, w);
+  for (int i = 0; i < p.t.n; ++i) SCR(x, i) = WROW(i);
 }
 
 // Sum over the block of one value per thread; every thread gets the same
@@ -237,7 +400,7 @@ __device__ double attempt(const SolveParams& p, const Lane& ln, double H, const 
       }
       WROW(i) = v;
     }
-    lu_solve(p, ln, lu, w);
+    solve_in_w(p, ln, lu, w);
     double* Kr = K + (int64_t)r * n * L;
     for (int i = 0; i < n; ++i) SCR(Kr, i) = WROW(i);
     ++c_solves;
@@ -273,6 +436,158 @@ __device__ void trace_record(const SolveParams& p, int g, int& nrec, double t, d
     rec[3] = outcome;
   }
   ++nrec;
+}
+
+// Block-wide max with NaN propagation (numpy max) and block-wide AND.
+__device__ double block_max(double v, double* red) {
+  for (int off = 16; off > 0; off >>= 1) v = npmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+  const int nw = blockDim.x >> 5;
+  if (nw == 1) return v;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = red[0];
+  for (int i = 1; i < nw; ++i) s = npmax(s, red[i]);
+  return s;
+}
+
+__device__ bool block_all(bool v) {
+  return __syncthreads_and(v ? 1 : 0) != 0;
+}
+
+struct ProjectionCounts {
+  long long rhs = 0, jac = 0, lu = 0, solves = 0, passes = 0, trials = 0;
+};
+
+// All algebraic entries of A (a per-lane vector) finite, over the group.
+__device__ bool alg_finite(const SolveParams& p, const Lane& ln, const double* A) {
+  const int L = ln.L, lane = ln.lane;
+  bool ok = true;
+  if (ln.active)
+    for (int i = 0; i < p.t.n; ++i)
+      if (__ldg(p.t.mass + i) == 0.0 && !isfinite(SCR(A, i))) ok = false;
+  return block_all(ok);
+}
+
+// max over the group's algebraic entries of |A|
+__device__ double alg_absmax(const SolveParams& p, const Lane& ln, const double* A, double* red) {
+  const int L = ln.L, lane = ln.lane;
+  double m = 0.0;
+  if (ln.active)
+    for (int i = 0; i < p.t.n; ++i)
+      if (__ldg(p.t.mass + i) == 0.0) m = npmax(m, fabs(SCR(A, i)));
+  return block_max(m, red);
+}
+
+// The weighted Newton correction of fastode/solvers.py:119-124:
+// max over algebraic entries of |d| / (atol + rtol max(|z|, |z + d|)), with
+// 0 where d = 0 and the scale vanishes, inf where only the scale vanishes.
+__device__ double weighted(const SolveParams& p, const Lane& ln, const double* Z, const double* D, double* red) {
+  const int L = ln.L, lane = ln.lane;
+  double m = 0.0;
+  if (ln.active)
+    for (int i = 0; i < p.t.n; ++i) {
+      if (__ldg(p.t.mass + i) != 0.0) continue;
+      const double z = SCR(Z, i), d = SCR(D, i);
+      const double scale =
+          __dadd_rn(__ldg(p.atol + __ldg(p.t.perm + i)), __dmul_rn(p.rtol, npmax(fabs(z), fabs(__dadd_rn(z, d)))));
+      double q;
+      if (scale > 0.0) q = __ddiv_rn(fabs(d), scale);
+      else if (scale != scale) q = scale;
+      else q = (d == 0.0) ? 0.0 : CUDART_INF;
+      m = npmax(m, q);
+    }
+  return block_max(m, red);
+}
+
+// G = F(Z) with the differential rows zeroed (fastode/solvers.py:110-114).
+__device__ void alg_residual(const SolveParams& p, const Lane& ln, const double* Z, double* rr, double* G) {
+  const int L = ln.L, lane = ln.lane;
+  eval_rhs(p, ln, Z, rr, G);
+  for (int i = 0; i < p.t.n; ++i)
+    if (__ldg(p.t.mass + i) != 0.0) SCR(G, i) = 0.0;
+}
+
+__device__ void factor_any(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
+                           double* w, bool alg_only);
+__device__ void solve_into(const SolveParams& p, const Lane& ln, const double* lu, double* w, const double* b,
+                           double* x);
+
+// Consistent initialization of the algebraic species, fastode/solvers.py:100-178:
+// damped Newton with the algebraic-rows-only matrix (alpha = 1), accepted on
+// the weighted correction, with backtracking line search. Returns true on
+// convergence; on failure Y is restored to its value on entry.
+__device__ __noinline__ bool project(const SolveParams& p, const Lane& ln, double* Y, double* scr, double* w, double* red,
+                        ProjectionCounts& pc) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n;
+  double* G = scr + p.sl.f0 * L;
+  double* cand = scr + p.sl.yr * L;
+  double* orig = scr + p.sl.ynew * L;
+  double* delta = scr + p.sl.k * L;
+  double* trial = scr + (p.sl.k + n) * L;
+  double* Gc = scr + p.sl.ft * L;
+  double* rr = scr + p.sl.r * L;
+  double* negj = scr + p.sl.negj * L;
+  double* dd = scr + p.sl.d * L;
+  double* lu = scr + p.sl.lu * L;
+  const int max_updates = 10, max_backtracks = 24;
+  const double tol = 0.1, factor_bt = 0.5, sigma = 1.0e-4;
+  bool have_orig = false;
+  for (int update = 0; update <= max_updates; ++update) {
+    alg_residual(p, ln, Y, rr, G);
+    ++pc.rhs;
+    if (!alg_finite(p, ln, G)) break;
+    ++pc.passes;
+    if (alg_absmax(p, ln, G, red) == 0.0) return true;
+    eval_negjac(p, ln, Y, dd, negj);
+    ++pc.jac;
+    factor_any(p, ln, 1.0, negj, lu, w, true);
+    ++pc.lu;
+    solve_into(p, ln, lu, w, G, delta);
+    ++pc.solves;
+    if (!alg_finite(p, ln, delta)) break;
+    const double q = weighted(p, ln, Y, delta, red);
+    if (q <= tol) return true;
+    if (update == max_updates) break;
+    if (!have_orig) {
+      for (int i = 0; i < n; ++i) SCR(orig, i) = SCR(Y, i);
+      have_orig = true;
+    }
+    double step = 1.0;
+    bool accepted = false;
+    for (int bt = 0; bt <= max_backtracks; ++bt) {
+      for (int i = 0; i < n; ++i) {
+        double v = SCR(Y, i);
+        if (__ldg(p.t.mass + i) == 0.0) v = __dadd_rn(v, __dmul_rn(step, SCR(delta, i)));
+        SCR(cand, i) = v;
+      }
+      const double step_used = step;
+      step = __dmul_rn(step, factor_bt);
+      if (!alg_finite(p, ln, cand)) continue;
+      alg_residual(p, ln, cand, rr, Gc);
+      ++pc.trials;
+      ++pc.rhs;
+      if (!alg_finite(p, ln, Gc)) continue;
+      if (alg_absmax(p, ln, Gc, red) == 0.0) {
+        accepted = true;
+        break;
+      }
+      solve_into(p, ln, lu, w, Gc, trial);
+      ++pc.solves;
+      if (!alg_finite(p, ln, trial)) continue;
+      const double qt = weighted(p, ln, cand, trial, red);
+      if (qt <= tol || qt < __dmul_rn(__dsub_rn(1.0, __dmul_rn(sigma, step_used)), q)) {
+        accepted = true;
+        break;
+      }
+    }
+    if (!accepted) break;
+    for (int i = 0; i < n; ++i) SCR(Y, i) = SCR(cand, i);
+  }
+  if (have_orig)
+    for (int i = 0; i < n; ++i) SCR(Y, i) = SCR(orig, i);
+  return false;
 }
 
 // One group over one interval: fastode/solvers.py:305-415 statement by statement.
@@ -320,7 +635,16 @@ __device__ void solve_group(const SolveParams& p, int g, double* scr, double* w,
   int nsteps = 0;
   int status = -1;  // running
   const double nsize = (double)(C * n);
-  while (__dadd_rn(__dsub_rn(t, dt), rounding) <= 0.0 && status < 0) {
+  ProjectionCounts pc;
+  if (p.t.has_constraints && !project(p, ln, Y, scr, w, red, pc)) {
+    status = FO_STATUS_PROJECTION_FAILED;   // Y restored, no step taken
+    proposed = h_next;                      // the carried proposal is left as it was
+  }
+  c_rhs += pc.rhs;
+  c_jac += pc.jac;
+  c_lu += pc.lu;
+  c_solves += pc.solves;
+  while (status < 0 && __dadd_rn(__dsub_rn(t, dt), rounding) <= 0.0) {
     if (nsteps >= o.max_steps) {
       status = FO_STATUS_TOO_MANY_STEPS;
       break;
@@ -347,7 +671,7 @@ __device__ void solve_group(const SolveParams& p, int g, double* scr, double* w,
         status = FO_STATUS_STEP_TOO_SMALL;
         break;
       }
-      factor(p, ln, 1.0 / __dmul_rn(H, o.tab.gamma), negj, lu, w);
+      factor_any(p, ln, 1.0 / __dmul_rn(H, o.tab.gamma), negj, lu, w, false);
       ++c_lu;
       const double part = attempt(p, ln, H, Y, Ynew, scr, w, c_rhs, c_solves);
       const double total = block_sum(part, red);
@@ -407,11 +731,13 @@ __device__ void solve_group(const SolveParams& p, int g, double* scr, double* w,
   }
   if (status < 0) status = FO_STATUS_CONVERGED;
 
-  // clamp (fastode/solvers.py:89-97) and write back
+  // clamp (fastode/solvers.py:89-97) and write back; a failed projection
+  // returns the restored state unclamped (fastode/solvers.py:323-325)
+  const bool clamp = status != FO_STATUS_PROJECTION_FAILED;
   if (ln.active) {
     for (int i = 0; i < n; ++i) {
       double y = SCR(Y, i);
-      if (!p.t.has_constraints || __ldg(p.t.mass + i) == 1.0) y = clamp0(y);
+      if (clamp && (!p.t.has_constraints || __ldg(p.t.mass + i) == 1.0)) y = clamp0(y);
       p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss] = y;
     }
   }
@@ -427,6 +753,8 @@ __device__ void solve_group(const SolveParams& p, int g, double* scr, double* w,
     cn[4] += c_jac;
     cn[5] += c_lu;
     cn[6] += c_solves;
+    cn[10] += pc.passes;
+    cn[11] += pc.trials;
     cn[12] += 1;
     p.status[g] = status;
     if (p.trace_len) p.trace_len[g] = nrec;

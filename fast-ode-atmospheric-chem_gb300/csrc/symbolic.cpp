@@ -275,6 +275,27 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
     t->lu_row_ptr.push_back((int32_t)t->lu_col.size());
   }
 
+  // elimination stream, row by row, each row padded to whole chunks
+  t->el_ptr.assign(1, 0);
+  t->el.clear();
+  for (int r = 0; r < n; ++r) {
+    size_t start = t->el.size();
+    for (int q = t->lu_row_ptr[r]; q < t->lu_diag[r]; ++q) {
+      const int k = t->lu_col[q];
+      t->el.push_back(-1 - t->lu_diag[k]);
+      t->el.push_back(k);
+      for (int u = t->lu_diag[k] + 1; u < t->lu_row_ptr[k + 1]; ++u) {
+        t->el.push_back(u);
+        t->el.push_back(t->lu_col[u]);
+      }
+    }
+    while (((t->el.size() - start) / 2) % kStreamChunk != 0) {
+      t->el.push_back(-1);
+      t->el.push_back(-1);
+    }
+    t->el_ptr.push_back((int32_t)(t->el.size() / 2));
+  }
+
   // Jacobian entries in assembly order
   std::vector<std::vector<std::pair<int, int>>> by_row(n);  // (perm col, original entry)
   for (int e = 0; e < m.nnz; ++e)

@@ -11,6 +11,9 @@
 
 namespace fo {
 
+// Entries per software-pipelined chunk of the elimination stream.
+constexpr int kStreamChunk = 16;
+
 // Everything the device needs, in the permuted species numbering
 // (p = 0..n-1 is the p-th eliminated species, perm[p] its original index).
 struct HostTables {
@@ -38,6 +41,14 @@ struct HostTables {
   std::vector<int32_t> lu_row_ptr, lu_diag, lu_col;
   // position of the Jacobian entry q inside the LU storage
   std::vector<int32_t> j_lu_pos;
+
+  // Elimination stream: for row r, entries el[2*t], el[2*t+1] for
+  // el_ptr[r] <= t < el_ptr[r+1], padded to a multiple of kStreamChunk.
+  //   update  (x >= 0):          w[y] -= l * lu[x]    (x: a U entry of an earlier row)
+  //   marker  (x < 0, y >= 0):   l = w[y] * lu[-1-x]  (y = k, -1-x = diagonal slot of row k,
+  //                              which holds 1/pivot); l is stored in the next L slot of row r
+  //   no-op   (x = -1, y = -1):  padding
+  std::vector<int32_t> el_ptr, el;
 
   int64_t lu_fma = 0, solve_fma = 0;
   int nnz_l = 0, nnz_u = 0;

@@ -84,7 +84,10 @@ class Algorithm:
     def __init__(self, tableau: Tableau = ROS3, controller: str = "h211b", b: float = 4.0,
                  safety: float = 0.9, fac_min: float = 0.2, fac_max: float = 6.0,
                  carry: bool = True, quantize: bool = True, max_steps: int = 1000,
-                 carry_memory: bool = True, ordering: str = "auto"):
+                 carry_memory: bool = True, ordering: str = "auto", kernel: str = "pipelined"):
+        """The reference's arguments, plus two of the device path: the
+        fill-reducing ``ordering`` of the sparse LU and the ``kernel`` variant
+        ("pipelined", the fast path, or "plain", the direct loops)."""
         self.tableau = tableau
         self.controller = controller
         self.b = b
@@ -96,6 +99,9 @@ class Algorithm:
         self.max_steps = max_steps
         self.carry_memory = carry_memory
         self.ordering = ordering
+        if kernel not in _abi.VARIANTS:
+            raise ValueError(f"kernel must be one of {sorted(_abi.VARIANTS)}")
+        self.kernel = kernel
         tableau_id(tableau)
 
     def new_memory(self) -> Memory:
@@ -115,7 +121,7 @@ class Algorithm:
         return _abi.Options(tableau_id(self.tableau), 0 if self.controller == "h211b" else 1,
                             float(self.b), float(self.safety), float(self.fac_min), float(self.fac_max),
                             int(bool(self.carry)), int(bool(self.quantize)), int(bool(self.carry_memory)),
-                            int(self.max_steps))
+                            int(self.max_steps), _abi.VARIANTS[self.kernel])
 
     def solve(self, system, Y, dt, atol, rtol, counts: Counts, memory: Memory = None):
         """Integrate one group (all rows of Y) over one interval; returns
@@ -131,7 +137,7 @@ class Algorithm:
             raise ValueError(f"Y has {n} species, the system {system.n}")
         plan = plan_for(system.mech, system.mass, self.ordering)
         k = _k_rows(system, C_cells)
-        atol = np.ascontiguousarray(np.broadcast_to(np.asarray(atol, dtype=np.float64), (n,)))
+        atol = np.array(np.broadcast_to(np.asarray(atol, dtype=np.float64), (n,)))
         mem = memory if memory is not None else Memory()
         dev = torch.device("cuda", plan.device)
         Yd = torch.from_numpy(np.ascontiguousarray(Y)).to(dev)

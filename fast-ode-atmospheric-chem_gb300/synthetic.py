@@ -148,6 +148,13 @@ class Workload:
         t = interval * self.dt if self.update_photolysis else 0.0
         return rate_constants(self.sm, self.cells, t)
 
+    def subset(self, sl: slice) -> "Workload":
+        """The same workload restricted to the cells of `sl`."""
+        c = self.cells
+        cells = SyntheticCells(c.T[sl].copy(), c.p[sl].copy(), c.phase[sl].copy(), c.Y0[sl].copy())
+        return Workload(self.name, self.sm, cells, self.dt, self.intervals, self.rtol, self.group_size,
+                        self.update_photolysis)
+
 
 def plain_small(n_cells: int = 64, intervals: int = 20, seed: int = 1) -> Workload:
     """Plain ROS3, 20 species / 40 reactions, 64 cells in groups of 32,

@@ -115,7 +115,15 @@ typedef struct fo_options {
   int32_t quantize;           /* round proposals to divisors of the interval */
   int32_t carry_memory;       /* keep the filter memory across intervals */
   int32_t max_steps;          /* attempt budget per call (1000) */
+  int32_t variant;            /* FO_VARIANT_*: which LU/solve kernel (same results up to roundoff) */
 } fo_options;
+
+/* Kernel variants of the factorization and solves. PIPELINED streams the
+ * elimination schedule with register double-buffering (the fast path);
+ * PLAIN is the direct row-by-row loop, kept as the baseline it is measured
+ * against. */
+#define FO_VARIANT_PIPELINED 0
+#define FO_VARIANT_PLAIN 1
 
 /* Host-only symbolic analysis: ordering, fill and flop counts, and (when
  * perm is not NULL) the elimination order perm[p] = species eliminated p-th.
@@ -188,6 +196,26 @@ int fo_eval_jac(const fo_plan* plan, int32_t C,
                 const double* Y, int64_t y_cell_stride, int64_t y_species_stride,
                 const double* k, int64_t k_cell_stride, int64_t k_reaction_stride,
                 double* J, void* stream);
+
+/* Thermal rate constants on the device: k[c, j] = A[j] exp(-E[j] / T[c]) *
+ * M[c]^power[j] (power may be NULL: no third bodies). The Arrhenius rows of
+ * fastode.ts1.TS1.rate_constants (fastode/ts1.py:76-79) with [M] folded in as
+ * fastode/ts1.py:100-102 folds it. Device pointers; asynchronous on stream. */
+int fo_rate_constants(int32_t C, int32_t R, const double* A, const double* E, const double* power,
+                      const double* T, const double* M, double* k,
+                      int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
+
+/* Photolysis columns at an interval start: k[c, rxn[p]] = J[p] *
+ * max(0, cos(phase[c] + omega * t)), the device form of the per-interval
+ * photolysis patch of fastode/ts1.py:204-214. Device pointers; asynchronous. */
+int fo_update_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const double* J,
+                         const double* phase, double omega, double t, double* k,
+                         int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
+
+/* FP64 fused multiply-add throughput of the current device (FMA per second),
+ * measured with a full-warp DFMA kernel: the roofline denominator for the
+ * integrator. No counterpart in the reference (which never times work). */
+int fo_fp64_fma_rate(double* fma_per_second);
 
 /* Last CUDA error text seen by the library (thread-local, never NULL). */
 const char* fo_last_error(void);

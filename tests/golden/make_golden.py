@@ -101,6 +101,55 @@ def run_reference(fastode_mod, wl, n_groups, intervals):
                 n_attempts=np.array([len(t[1]) for t in traces]))
 
 
+def mechanism_arrays(mech):
+    """The reference Mechanism's compiled tables (fastode/chem.py:19-79)."""
+    GT = mech.GT.tocsr()
+    return dict(m_n=mech.n, m_R=mech.R, m_P=mech.P, m_react=mech.react, m_S=mech.S,
+                m_rows=mech.pattern.rows, m_cols=mech.pattern.cols,
+                m_gt_indptr=GT.indptr, m_gt_indices=GT.indices, m_gt_data=GT.data)
+
+
+def dae_cases():
+    """RODAS3 with quasi-steady species (mass = 0), the reference's own small
+    mechanisms of fastode/problems.py run through Algorithm.solve, which then
+    starts every call with the consistent-initialization projection
+    (fastode/solvers.py:100-178, 322-325)."""
+    from fastode import Algorithm, Counts, RODAS3
+    from fastode import problems as P
+    from fastode.chem import ChemSystem
+    out = {}
+    specs = {
+        # name: (system, Y0, dt, atol, rtol, intervals); tropospheric gets four
+        # cells that differ in photolysis (j = 1, 0.5, 0.1, 0.02)
+        "rodas3_robertson_qssa": (P.robertson(qssa=True), 1.0, 1e-10, 1e-4, 6),
+        "rodas3_chapman_qssa": (P.chapman(qssa=True), 3600.0, 1e-6, 1e-4, 24),
+        "rodas3_tropospheric_qssa": (None, 600.0, 600.0, 1e-3, 24),
+    }
+    for name, (made, dt, atol, rtol, intervals) in specs.items():
+        if made is None:
+            cells = [P.tropospheric(j=j, qssa=True) for j in (1.0, 0.5, 0.1, 0.02)]
+            mech = cells[0][0].mech
+            mass = cells[0][0].mass
+            k = np.concatenate([c[0].k for c in cells])
+            Y0 = np.concatenate([c[1] for c in cells])
+        else:
+            system, Y0 = made
+            mech, mass, k = system.mech, system.mass, system.k
+        alg = Algorithm(RODAS3)
+        mem = alg.new_memory()
+        c = Counts()
+        Y = Y0.copy()
+        atolv = np.full(mech.n, atol)
+        status = []
+        for _ in range(intervals):
+            Y, st = alg.solve(ChemSystem(mech, k, mass=mass), Y, dt, atolv, rtol, c, mem)
+            status.append(STATUS[st])
+        out[name] = dict(mechanism_arrays(mech), mass=mass, k=k, Y0=Y0, dt=dt, atol=atolv, rtol=rtol,
+                         intervals=intervals, Y=Y, counts=np.array(list(c.as_dict().values())),
+                         status=np.array(status), memory=np.array([mem.h_next, mem.err_prev, mem.h_prev]))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -109,6 +158,10 @@ def main():
     sys.path.insert(0, str(ROOT))
     import fastode
     from fastode_gb300 import synthetic as syn
+
+    for name, arrays in dae_cases().items():
+        np.savez_compressed(HERE / f"{name}.npz", **arrays)
+        print(name, "counts", arrays["counts"].tolist(), "status", arrays["status"].tolist())
 
     cases = {
         # name: (workload, groups, intervals)

@@ -35,3 +35,35 @@ def mechanism_of(f):
 def rel_err(y, ref, floor=A_FLOOR):
     """|y - ref| / max(|ref|, a), elementwise."""
     return np.abs(y - ref) / np.maximum(np.abs(ref), floor)
+
+
+DAE_CASES = ("rodas3_robertson_qssa", "rodas3_chapman_qssa", "rodas3_tropospheric_qssa")
+
+
+class _Pattern:
+    def __init__(self, rows, cols):
+        self.rows = np.asarray(rows, dtype=np.int64)
+        self.cols = np.asarray(cols, dtype=np.int64)
+        self.nnz = len(self.rows)
+
+
+class TableMechanism:
+    """A mechanism given by the reference's compiled tables (react, S,
+    pattern, GT map) as stored in a fixture."""
+
+    def __init__(self, f):
+        self.n, self.R, self.P = int(f["m_n"]), int(f["m_R"]), int(f["m_P"])
+        self.react = np.asarray(f["m_react"], dtype=np.int64)
+        self.S = np.asarray(f["m_S"], dtype=np.float64)
+        self.pattern = _Pattern(f["m_rows"], f["m_cols"])
+        self._gt = (np.asarray(f["m_gt_indptr"], np.int32), np.asarray(f["m_gt_indices"], np.int32),
+                    np.asarray(f["m_gt_data"], np.float64))
+        self.species = [f"y{i}" for i in range(self.n)]
+
+    def jac_csr(self):
+        return tuple(a.copy() for a in self._gt)
+
+    def dense_jacobian(self, vals):
+        J = np.zeros((vals.shape[0], self.n, self.n))
+        J[:, self.pattern.rows, self.pattern.cols] = vals
+        return J

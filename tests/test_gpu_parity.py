@@ -4,8 +4,10 @@ the reference itself) and with the oracle, through the C-ABI.
 The bar (the reference's own outputs on the same inputs):
   * Counts per group and status per group and interval: identical;
   * the attempted step sizes: identical (they are quantized divisors of dt);
-  * the error norm per attempt: within 1e-8 relative (the device LU is
-    pivot-free in its own order, SuperLU pivots, so roundoff differs);
+  * the error norm per attempt: within 1e-8 relative plus 1e-7 absolute, in
+    units of the acceptance threshold err < 1 (the device LU is pivot-free in
+    its own order, SuperLU pivots, so roundoff differs; an error norm near
+    1e-10 is itself roundoff and may differ in its leading digits);
   * final states: within 1e-10 relative, floored at a = 1e-14.
 """
 import numpy as np
@@ -17,14 +19,16 @@ pytestmark = pytest.mark.gpu
 
 STATE_RTOL = 1e-10
 ERR_RTOL = 1e-8
+ERR_ATOL = 1e-7
 
 
-def run_batch(cuda, f, trace_cap=64, slots=0, group_size=None):
+def run_batch(cuda, f, trace_cap=64, slots=0, group_size=None, kernel="pipelined"):
+    from fastode_gb300 import Algorithm
     from fastode_gb300.batch import Batch
     torch = cuda
     mech = mechanism_of(f)
     gs = int(f["group_size"]) if group_size is None else group_size
-    b = Batch(mech, f["Y0"], group_size=gs, trace_cap=trace_cap, slots=slots)
+    b = Batch(mech, f["Y0"], group_size=gs, trace_cap=trace_cap, slots=slots, algorithm=Algorithm(kernel=kernel))
     atol = torch.from_numpy(f["atol"]).cuda()
     traces = [[] for _ in range(b.ngroups)]
     statuses = []
@@ -43,22 +47,23 @@ def run_batch(cuda, f, trace_cap=64, slots=0, group_size=None):
 
 
 @pytest.mark.parametrize("case", CASES)
-def test_device_matches_reference_fixture(cuda, case):
+@pytest.mark.parametrize("kernel", ["pipelined", "plain"])
+def test_device_matches_reference_fixture(cuda, case, kernel):
     f = load(case)
-    b, statuses, traces = run_batch(cuda, f)
+    b, statuses, traces = run_batch(cuda, f, kernel=kernel)
     counts = b.counts.cpu().numpy()
     np.testing.assert_array_equal(counts, f["counts"])
     np.testing.assert_array_equal(statuses, f["status"])
     mem = b.memory.cpu().numpy()
     np.testing.assert_array_equal(mem[:, 0], f["memory"][:, 0])      # h_next: quantized
     np.testing.assert_array_equal(mem[:, 2], f["memory"][:, 2])      # h_prev
-    np.testing.assert_allclose(mem[:, 1], f["memory"][:, 1], rtol=ERR_RTOL)
+    np.testing.assert_allclose(mem[:, 1], f["memory"][:, 1], rtol=ERR_RTOL, atol=ERR_ATOL)
     for g in range(b.ngroups):
         na = int(f["n_attempts"][g])
         tr = np.array(traces[g])
         assert len(tr) == na
         np.testing.assert_array_equal(tr[:, 1], f["hs"][g, :na])
-        np.testing.assert_allclose(tr[:, 2], f["errs"][g, :na], rtol=ERR_RTOL)
+        np.testing.assert_allclose(tr[:, 2], f["errs"][g, :na], rtol=ERR_RTOL, atol=ERR_ATOL)
         np.testing.assert_array_equal(tr[:, 3], (f["errs"][g, :na] < 1.0).astype(float))
     Y = b.state()
     assert rel_err(Y, f["Y"]).max() <= STATE_RTOL
@@ -109,9 +114,14 @@ def test_rhs_and_jacobian_match_oracle(cuda, case):
     k = f["k"][0]
     ours = ChemSystem(mech, k, dense=False)
     ref = OChem(mech, k, dense=False)
-    # Jacobian values: same products and the same summation order as the
-    # reference's CSR map: bit-identical
-    np.testing.assert_array_equal(ours.jac(Y), ref.jac_values(Y))
+    # Jacobian values: the same products summed in the reference's CSR order;
+    # SciPy's compiled matvec may contract into FMA, so allow a few ulps of the
+    # absolute sum of the terms
+    J, Jr = ours.jac(Y), ref.jac_values(Y)
+    absref = OChem(mech, np.abs(k), dense=False)
+    absref.GT = abs(ref.GT)
+    jscale = absref.jac_values(np.abs(Y))
+    assert np.all(np.abs(J - Jr) <= 4e-16 * 8 * jscale + 1e-300)
     # forcing: the reference sums with a BLAS GEMM, the device in CSR order
     F, Fr = ours.rhs(Y), ref.rhs(Y)
     scale = np.abs(ref.rates(Y)) @ np.abs(ref.ST)

@@ -90,7 +90,7 @@ def test_mechanism_tables_match_reference(case):
 def declared_symbols():
     text = (ROOT / "include" / "fastode_gb300.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(fo_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(fo_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_library_exports_every_declared_symbol(built_library):
