@@ -167,13 +167,14 @@ def run_ours(args, rank, world):
 
     thermal()
     Y0 = torch.from_numpy(cells.Y0).to(dev)
-    batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots)
+    from fastode_gb300 import Algorithm
+    batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel=args.kernel))
 
-    def reset():
-        batch.Y.copy_(Y0.t())
-        batch.memory.zero_()
-        batch.counts.zero_()
-        batch.status.zero_()
+    def reset(b=batch):
+        b.Y.copy_(Y0.t())
+        b.memory.zero_()
+        b.counts.zero_()
+        b.status.zero_()
 
     for i in range(args.warmup):                     # untimed: the same kernels and shapes
         photolysis(i)
@@ -185,9 +186,11 @@ def run_ours(args, rank, world):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with Clocks(dev.index) as clocks:
         start.record()
         for i in range(args.steps):
+            marks[i].record()
             photolysis(i)
             ev[i][0].record()
             batch.step(k, wl.dt, d["atol"], wl.rtol)
@@ -195,6 +198,30 @@ def run_ours(args, rank, world):
         end.record()
         torch.cuda.synchronize()
     elapsed = start.elapsed_time(end) / 1e3
+    interval_ms = [marks[i].elapsed_time(marks[i + 1] if i + 1 < args.steps else end) for i in range(args.steps)]
+
+    # the plain one-group-per-block kernel (FO_VARIANT_PLAIN) on the first
+    # intervals of the same job, for the "vs plain GPU" comparison
+    plain = None
+    n_plain = min(args.plain_steps, args.steps)
+    if n_plain > 0 and args.kernel != "plain":
+        pb = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel="plain"))
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record()
+        for i in range(n_plain):
+            photolysis(i)
+            pb.step(k, wl.dt, d["atol"], wl.rtol)
+        p1.record()
+        torch.cuda.synchronize()
+        plain_s = p0.elapsed_time(p1) / 1e3
+        ours_s = sum(interval_ms[:n_plain]) / 1e3
+        plain = {"value": Cc * n_plain / plain_s, "unit": "cell-intervals/s", "intervals": n_plain,
+                 "ours_same_intervals": Cc * n_plain / ours_s, "speedup": plain_s / ours_s,
+                 "same_counts": bool(np.array_equal(pb.counts.cpu().numpy().sum(0),
+                                                    batch.counts.cpu().numpy().sum(0))) if n_plain == args.steps
+                 else None}
+        del pb
     if world > 1:
         t = torch.tensor([elapsed], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -252,6 +279,10 @@ def run_ours(args, rank, world):
                      "algorithmic_flops_per_launch": flops / args.steps},
         "clocks": clocks.summary(),
         "e2e": e2e,
+        "plain_gpu": plain,
+        "kernel_variant": args.kernel,
+        "interval_ms": {"first": interval_ms[0], "median": float(np.median(interval_ms)),
+                        "max": float(max(interval_ms))},
     }
     if rank == 0 and args.cpu_intervals > 0 and not args.no_cpu:
         workers = args.cpu_workers or os.cpu_count()
@@ -301,6 +332,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--cells", type=int, default=65536)
     ap.add_argument("--slots", type=int, default=0)
+    ap.add_argument("--kernel", default="pipelined", choices=["pipelined", "plain"])
+    ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--cpu-intervals", type=int, default=30)

@@ -33,6 +33,19 @@ def test_rodas3_projection_matches_reference(cuda, case, kernel):
         status.append(st)
     names = ("converged", "too many steps", "step too small", "nan or inf", "projection failed")
     assert [names.index(s) for s in status] == list(f["status"])
-    assert tuple(c.as_dict().values()) == tuple(f["counts"])
+    got = np.array(list(c.as_dict().values()))
+    ref = np.asarray(f["counts"])
+    # A call whose projection residual the reference evaluates to exactly 0.0
+    # returns before the Newton update. That equality is a bit-level tie: the
+    # reference sums the forcing with a BLAS GEMM, the device in CSR order, so
+    # the device may take the one Newton update (Jacobian, factorization,
+    # solve) such a call skips; its correction is at roundoff level and does
+    # not change the result. Only those calls may differ, only by that.
+    ties = int(f["zero_residual_calls"])
+    extra = got - ref
+    jac_lu_solve = [4, 5, 6]
+    assert np.all(extra[[i for i in range(13) if i not in jac_lu_solve]] == 0), (got, ref)
+    assert np.all((extra[jac_lu_solve] >= 0) & (extra[jac_lu_solve] <= ties)), (got, ref)
+    assert extra[4] == extra[5] == extra[6]
     assert mem.h_next == f["memory"][0]
     assert rel_err(Y, f["Y"], floor=1e-300 + np.abs(f["atol"]).max() * 1e-4).max() <= 1e-9
