@@ -52,6 +52,15 @@ class Options(C.Structure):
 VARIANTS = {"pipelined": 0, "plain": 1}
 
 
+class BatchDesc(C.Structure):
+    _fields_ = [("plan", C.c_void_p), ("opt", Options), ("ngroups", C.c_int32),
+                ("group_offsets", C.c_void_p), ("max_group_cells", C.c_int32),
+                ("Y", C.c_void_p), ("y_cell_stride", C.c_int64), ("y_species_stride", C.c_int64),
+                ("k", C.c_void_p), ("k_cell_stride", C.c_int64), ("k_reaction_stride", C.c_int64),
+                ("atol", C.c_void_p), ("rtol", C.c_double), ("dt", C.c_double),
+                ("memory", C.c_void_p), ("counts", C.c_void_p), ("status", C.c_void_p)]
+
+
 _P = C.c_void_p
 _I32 = C.c_int32
 _I64 = C.c_int64
@@ -74,6 +83,12 @@ SIGNATURES = {
     "fo_rate_constants": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
     "fo_update_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _D, _P, _I64, _I64, _P]),
     "fo_fp64_fma_rate": (C.c_int, [C.POINTER(C.c_double)]),
+    "fo_multi_workspace_bytes": (C.c_int, [_I32, C.POINTER(BatchDesc), _I32, C.POINTER(C.c_size_t)]),
+    "fo_multi_prepare": (C.c_int, [_I32, C.POINTER(BatchDesc), _P, C.c_size_t, _I32, C.POINTER(_P)]),
+    "fo_multi_launch": (C.c_int, [_P, _P]),
+    "fo_multi_destroy": (C.c_int, [_P]),
+    "fo_update_photolysis_clock": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _P, _P, _I64, _I64, _P]),
+    "fo_advance_clock": (C.c_int, [_P, _D, _P]),
 }
 
 _lib = None

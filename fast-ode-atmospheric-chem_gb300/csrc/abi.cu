@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -16,6 +17,9 @@
 namespace fo {
 cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream);
 cudaError_t launch_eval(const SolveParams& p, int C, int want_jac, double* out, cudaStream_t stream);
+cudaError_t launch_solve_multi(const SolveParams* batches, int nb, const int32_t* starts, int32_t* queue,
+                               double* scratch, int64_t slot_doubles, int grid, int lanes, size_t smem,
+                               cudaStream_t stream);
 }  // namespace fo
 
 struct fo_plan {
@@ -80,7 +84,17 @@ fo::ScratchLayout layout_of(const fo::HostTables& t) {
 
 int lanes_for(int cells) { return ((cells + 31) / 32) * 32; }
 
-size_t smem_bytes(const fo::HostTables& t, int lanes) { return sizeof(double) * (32 + (size_t)t.n * lanes); }
+// Shared-memory items per lane: the solve vector (n), or the compressed work
+// row plus the prefetch ring of the pipelined factorization, whichever is
+// larger (the two phases never overlap).
+int region_items(const fo::HostTables& t) {
+  const int ring = fo::kRingChunks * fo::kStreamChunk;
+  return t.n > t.max_row_len + ring ? t.n : t.max_row_len + ring;
+}
+
+size_t smem_bytes(const fo::HostTables& t, int lanes) {
+  return sizeof(double) * (32 + (size_t)region_items(t) * lanes);
+}
 
 constexpr size_t kHeader = 256;  // queue counter at the start of the workspace
 constexpr int kMaxLanes = 256;
@@ -108,7 +122,7 @@ void fill_info(const fo::HostTables& t, fo_plan_info* info) {
   info->jac_terms = (int32_t)t.jt_idx.size();
   info->stoich_nnz = (int32_t)t.s_rxn.size();
   info->scratch_doubles_per_cell = layout_of(t).items;
-  info->smem_doubles_per_cell = t.n;
+  info->smem_doubles_per_cell = region_items(t);
 }
 
 fo::SolveParams base_params(const fo_plan* plan) {
@@ -161,7 +175,8 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
          o_jrow = append(buf, t.j_row_ptr), o_jcol = append(buf, t.j_col), o_jsrc = append(buf, t.j_src),
          o_jtp = append(buf, t.jt_ptr), o_jti = append(buf, t.jt_idx), o_jtv = append(buf, t.jt_val),
          o_lur = append(buf, t.lu_row_ptr), o_lud = append(buf, t.lu_diag), o_luc = append(buf, t.lu_col),
-         o_elp = append(buf, t.el_ptr), o_el = append(buf, t.el);
+         o_elp = append(buf, t.el_ptr), o_el = append(buf, t.el), o_sf = append(buf, t.sf),
+         o_sb = append(buf, t.sb), o_jpos = append(buf, t.j_lu_pos), o_elpk = append(buf, t.elp);
   cudaError_t e = cudaGetDevice(&plan->device);
   if (e != cudaSuccess) {
     delete plan;
@@ -202,6 +217,14 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
   d.lu_col = reinterpret_cast<const int32_t*>(b + o_luc);
   d.el_ptr = reinterpret_cast<const int32_t*>(b + o_elp);
   d.el = reinterpret_cast<const int2*>(b + o_el);
+  d.elp = t.elp.empty() ? nullptr : reinterpret_cast<const uint32_t*>(b + o_elpk);
+  d.sf = reinterpret_cast<const int2*>(b + o_sf);
+  d.sb = reinterpret_cast<const int2*>(b + o_sb);
+  d.nsf = (int)(t.sf.size() / 2);
+  d.nsb = (int)(t.sb.size() / 2);
+  d.j_pos = reinterpret_cast<const int32_t*>(b + o_jpos);
+  d.max_row_len = t.max_row_len;
+  d.region = region_items(t);
   d.has_constraints = 0;
   for (double m : t.mass)
     if (m == 0.0) d.has_constraints = 1;
@@ -235,16 +258,22 @@ int fo_workspace_bytes(const fo_plan* plan, int32_t slots, int32_t max_group_cel
   return FO_OK;
 }
 
-int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
-             int32_t max_group_cells, double* Y, int64_t y_cell_stride, int64_t y_species_stride, const double* k,
-             int64_t k_cell_stride, int64_t k_reaction_stride, const double* atol, double rtol, double dt,
-             double* memory, int64_t* counts, int32_t* status, void* workspace, size_t workspace_bytes,
-             int32_t slots, double* trace, int32_t trace_cap, int32_t* trace_len, void* stream) {
-  if (!plan || !opt || !group_offsets || !Y || !k || !atol || !memory || !counts || !status || !workspace)
+}  // extern "C"
+
+namespace {
+
+// Validate one batch and fill its kernel parameters (everything but the
+// scratch and queue pointers).
+int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
+                int32_t max_group_cells, double* Y, int64_t ycs, int64_t yss, const double* k, int64_t kcs,
+                int64_t krs, const double* atol, double rtol, double dt, double* memory, int64_t* counts,
+                int32_t* status, fo::SolveParams* out, size_t* smem_out) {
+  if (!plan || !opt || !group_offsets || !Y || !k || !atol || !memory || !counts || !status)
     return fail(FO_E_INVALID, "null argument");
-  if (ngroups <= 0) return FO_OK;
   if (opt->tableau != FO_TABLEAU_ROS3 && opt->tableau != FO_TABLEAU_RODAS3)
     return fail(FO_E_INVALID, "unknown tableau");
+  if (opt->variant != FO_VARIANT_PIPELINED && opt->variant != FO_VARIANT_PLAIN)
+    return fail(FO_E_INVALID, "unknown kernel variant");
   if (max_group_cells <= 0 || max_group_cells > kMaxLanes)
     return fail(FO_E_UNSUPPORTED, "group size must be 1..256 cells");
   if (!(dt > 0.0)) return fail(FO_E_INVALID, "dt must be positive");
@@ -258,11 +287,6 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
   if (smem > (size_t)smem_max)
     return fail(FO_E_UNSUPPORTED, "species x group size exceed shared memory: use smaller groups");
-  const int grid = slots > 0 ? (slots < ngroups ? slots : ngroups) : ngroups;
-  size_t need = 0;
-  fo_workspace_bytes(plan, grid, max_group_cells, &need);
-  if (workspace_bytes < need) return fail(FO_E_WORKSPACE, "workspace too small");
-
   fo::SolveParams p = base_params(plan);
   p.o.tab = kTableaus[opt->tableau];
   p.o.controller = opt->controller;
@@ -275,17 +299,18 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   p.o.carry_memory = opt->carry_memory;
   p.o.max_steps = opt->max_steps;
   p.o.variant = opt->variant;
-  if (opt->variant != FO_VARIANT_PIPELINED && opt->variant != FO_VARIANT_PLAIN)
-    return fail(FO_E_INVALID, "unknown kernel variant");
+  // the pipelined kernel needs the packed stream (positions below 65,536 and
+  // rows shorter than 32,767 entries); larger mechanisms run the plain loops
+  if (p.o.variant == FO_VARIANT_PIPELINED && plan->dev.elp == nullptr) p.o.variant = FO_VARIANT_PLAIN;
   p.o.k_exp = 3.0;  // embedded order 2 for both tableaus
   p.ngroups = ngroups;
   p.group_offsets = group_offsets;
   p.Y = Y;
-  p.ycs = y_cell_stride;
-  p.yss = y_species_stride;
+  p.ycs = ycs;
+  p.yss = yss;
   p.k = k;
-  p.kcs = k_cell_stride;
-  p.krs = k_reaction_stride;
+  p.kcs = kcs;
+  p.krs = krs;
   p.atol = atol;
   p.rtol = rtol;
   p.dt = dt;
@@ -294,11 +319,76 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   p.status = status;
   p.lanes = lanes;
   p.slot_doubles = p.sl.items * lanes;
+  *out = p;
+  *smem_out = smem;
+  return FO_OK;
+}
+
+}  // namespace
+
+struct fo_multi {
+  int nb = 0, grid = 0, lanes = 0;
+  size_t smem = 0;
+  fo::SolveParams* d_batches = nullptr;  // in the workspace
+  int32_t* d_starts = nullptr;
+  int32_t* d_queue = nullptr;
+  double* d_scratch = nullptr;
+  int64_t slot_doubles = 0;
+};
+
+namespace {
+
+struct MultiLayout {
+  int lanes = 0, total = 0, grid = 0;
+  int64_t items = 0;
+  size_t params_off = 0, starts_off = 0, scratch_off = 0, bytes = 0;
+};
+
+int multi_layout(int32_t nb, const fo_batch_desc* b, int32_t slots, MultiLayout* L) {
+  if (nb <= 0 || !b) return fail(FO_E_INVALID, "no batches");
+  for (int i = 0; i < nb; ++i) {
+    if (!b[i].plan) return fail(FO_E_INVALID, "null plan");
+    if (b[i].ngroups < 0) return fail(FO_E_INVALID, "negative group count");
+    if (b[i].max_group_cells <= 0 || b[i].max_group_cells > kMaxLanes)
+      return fail(FO_E_UNSUPPORTED, "group size must be 1..256 cells");
+    L->lanes = std::max(L->lanes, lanes_for(b[i].max_group_cells));
+    L->items = std::max<int64_t>(L->items, layout_of(b[i].plan->host).items);
+    L->total += b[i].ngroups;
+  }
+  L->grid = slots > 0 ? std::min(slots, std::max(L->total, 1)) : std::max(L->total, 1);
+  L->params_off = kHeader;
+  L->starts_off = (L->params_off + sizeof(fo::SolveParams) * nb + 255) & ~size_t(255);
+  L->scratch_off = (L->starts_off + sizeof(int32_t) * (nb + 1) + 255) & ~size_t(255);
+  L->bytes = L->scratch_off + sizeof(double) * (size_t)L->grid * (size_t)L->items * L->lanes;
+  return FO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
+             int32_t max_group_cells, double* Y, int64_t y_cell_stride, int64_t y_species_stride, const double* k,
+             int64_t k_cell_stride, int64_t k_reaction_stride, const double* atol, double rtol, double dt,
+             double* memory, int64_t* counts, int32_t* status, void* workspace, size_t workspace_bytes,
+             int32_t slots, double* trace, int32_t trace_cap, int32_t* trace_len, void* stream) {
+  if (!workspace) return fail(FO_E_INVALID, "null workspace");
+  if (ngroups <= 0) return FO_OK;
+  fo::SolveParams p;
+  size_t smem = 0;
+  int rc = fill_params(plan, opt, ngroups, group_offsets, max_group_cells, Y, y_cell_stride, y_species_stride, k,
+                       k_cell_stride, k_reaction_stride, atol, rtol, dt, memory, counts, status, &p, &smem);
+  if (rc != FO_OK) return rc;
+  const int grid = slots > 0 ? (slots < ngroups ? slots : ngroups) : ngroups;
+  size_t need = 0;
+  fo_workspace_bytes(plan, grid, max_group_cells, &need);
+  if (workspace_bytes < need) return fail(FO_E_WORKSPACE, "workspace too small");
   p.scratch = reinterpret_cast<double*>(static_cast<char*>(workspace) + kHeader);
   p.trace = trace;
   p.trace_cap = trace ? trace_cap : 0;
   p.trace_len = trace_len;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
   if (slots > 0) {
     p.queue = static_cast<int32_t*>(workspace);
     e = cudaMemsetAsync(workspace, 0, sizeof(int32_t), s);
@@ -308,6 +398,91 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   }
   e = fo::launch_solve(p, grid, smem, s);
   if (e != cudaSuccess) return cuda_fail(e, "solve kernel launch");
+  return FO_OK;
+}
+
+int fo_multi_workspace_bytes(int32_t nbatches, const fo_batch_desc* batches, int32_t slots, size_t* bytes) {
+  if (!bytes) return fail(FO_E_INVALID, "null argument");
+  MultiLayout L;
+  int rc = multi_layout(nbatches, batches, slots, &L);
+  if (rc != FO_OK) return rc;
+  *bytes = L.bytes;
+  return FO_OK;
+}
+
+int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t workspace_bytes, int32_t slots,
+                     fo_multi** out) {
+  if (!out || !workspace) return fail(FO_E_INVALID, "null argument");
+  *out = nullptr;
+  MultiLayout L;
+  int rc = multi_layout(nb, b, slots, &L);
+  if (rc != FO_OK) return rc;
+  if (workspace_bytes < L.bytes) return fail(FO_E_WORKSPACE, "workspace too small");
+  // largest mechanisms first, so the queue's tail holds the cheapest groups
+  std::vector<int> order(nb);
+  for (int i = 0; i < nb; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return layout_of(b[x].plan->host).items > layout_of(b[y].plan->host).items;
+  });
+  std::vector<fo::SolveParams> params(nb);
+  std::vector<int32_t> starts(nb + 1, 0);
+  size_t smem = 0;
+  for (int j = 0; j < nb; ++j) {
+    const fo_batch_desc& d = b[order[j]];
+    size_t sm = 0;
+    rc = fill_params(d.plan, &d.opt, d.ngroups, d.group_offsets, d.max_group_cells, d.Y, d.y_cell_stride,
+                     d.y_species_stride, d.k, d.k_cell_stride, d.k_reaction_stride, d.atol, d.rtol, d.dt, d.memory,
+                     d.counts, d.status, &params[j], &sm);
+    if (rc != FO_OK) return rc;
+    smem = std::max(smem, sizeof(double) * (32 + (size_t)region_items(d.plan->host) * L.lanes));
+    starts[j + 1] = starts[j] + d.ngroups;
+  }
+  int dev = 0, smem_max = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  if (smem > (size_t)smem_max) return fail(FO_E_UNSUPPORTED, "species x group size exceed shared memory");
+  char* ws = static_cast<char*>(workspace);
+  fo_multi* m = new (std::nothrow) fo_multi;
+  if (!m) return fail(FO_E_ALLOC, "host allocation failed");
+  m->nb = nb;
+  m->grid = L.grid;
+  m->lanes = L.lanes;
+  m->smem = smem;
+  m->d_batches = reinterpret_cast<fo::SolveParams*>(ws + L.params_off);
+  m->d_starts = reinterpret_cast<int32_t*>(ws + L.starts_off);
+  m->d_queue = reinterpret_cast<int32_t*>(ws);
+  m->d_scratch = reinterpret_cast<double*>(ws + L.scratch_off);
+  m->slot_doubles = L.items * L.lanes;
+  for (auto& p : params) {
+    p.scratch = m->d_scratch;
+    p.slot_doubles = m->slot_doubles;
+    p.lanes = L.lanes;
+    p.queue = m->d_queue;
+  }
+  e = cudaMemcpy(m->d_batches, params.data(), sizeof(fo::SolveParams) * nb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->d_starts, starts.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete m;
+    return cuda_fail(e, "cudaMemcpy(batch table)");
+  }
+  *out = m;
+  return FO_OK;
+}
+
+int fo_multi_launch(const fo_multi* m, void* stream) {
+  if (!m) return fail(FO_E_INVALID, "null argument");
+  cudaError_t e = fo::launch_solve_multi(m->d_batches, m->nb, m->d_starts, m->d_queue, m->d_scratch,
+                                         m->slot_doubles, m->grid, m->lanes, m->smem,
+                                         static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "multi solve launch");
+  return FO_OK;
+}
+
+int fo_multi_destroy(fo_multi* m) {
+  delete m;
   return FO_OK;
 }
 

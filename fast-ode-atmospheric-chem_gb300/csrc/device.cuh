@@ -3,6 +3,8 @@
 
 #include <cstdint>
 
+#include "stream.h"
+
 namespace fo {
 
 // Index tables of one plan (device pointers), in the permuted numbering.
@@ -25,6 +27,13 @@ struct DevTables {
   const int32_t* lu_col;      // nlu
   const int32_t* el_ptr;      // n+1: elimination stream rows (entries)
   const int2* el;             // stream entries (x, y)
+  const uint32_t* elp;        // the stream packed to 32 bits, or null
+  const int2* sf;             // forward-solve stream
+  const int2* sb;             // backward-solve stream
+  int nsf, nsb;               // entries of each solve stream
+  const int32_t* j_pos;       // nnzj: position of each Jacobian entry in the LU storage
+  int max_row_len;            // longest row of the filled pattern
+  int region;                 // shared-memory items per lane (work row / ring / solve vector)
   int has_constraints;
 };
 

@@ -89,7 +89,7 @@ __device__ void eval_forcing(const SolveParams& p, const Lane& ln, const double*
   }
 }
 
-__device__ void eval_rhs(const SolveParams& p, const Lane& ln, const double* x, double* r, double* f) {
+__device__ __noinline__ void eval_rhs(const SolveParams& p, const Lane& ln, const double* x, double* r, double* f) {
   eval_rates(p, ln, x, r);
   eval_forcing(p, ln, r, f);
 }
@@ -97,7 +97,8 @@ __device__ void eval_rhs(const SolveParams& p, const Lane& ln, const double* x, 
 // Negated Jacobian values in assembly order: d[j,p] = k_j prod_{q != p} x_q,
 // then -J = sum of (-S[i,j]) d[j,p] over the map's terms
 // (fastode/chem.py:92-102).
-__device__ void eval_negjac(const SolveParams& p, const Lane& ln, const double* x, double* d, double* negj) {
+__device__ __noinline__ void eval_negjac(const SolveParams& p, const Lane& ln, const double* x, double* d,
+                                         double* negj) {
   const int L = ln.L, lane = ln.lane;
   const int n = p.t.n, R = p.t.R, P = p.t.P;
   const double* kc = p.k + ln.cell * p.kcs;
@@ -179,131 +180,197 @@ __device__ __noinline__ void factor(const SolveParams& p, const Lane& ln, double
 }
 
 // The same factorization driven by the precomputed elimination stream
-// (symbolic.h): every row's updates and multipliers are one flat sequence of
-// (x, y) entries, processed in chunks of kChunk with the next chunk's loads
-// (U entries of finished rows and pivot reciprocals, which no entry of the
-// row writes) issued before the current chunk computes. The warp keeps
-// kChunk 256-byte loads in flight while its FP64 pipe works.
-constexpr int kChunk = 16;
+// (symbolic.h): every row's multipliers and updates are one flat sequence of
+// (x, y) entries in chunks of kChunk. The work row is compressed to the row's
+// own pattern (w[y] stands for lu[row start + y]), which leaves room in shared
+// memory for a ring of kRingChunks chunks: each lane copies its own 8-byte U
+// entries (of finished rows, or pivot reciprocals — nothing the row writes)
+// into the ring with cp.async several chunks ahead of their use, so a warp
+// keeps up to (kRingChunks - 1) * kChunk 256-byte loads in flight without
+// holding them in registers.
+constexpr int kChunk = kStreamChunk;
 
-__device__ __forceinline__ void stream_load(const int2* __restrict__ meta, const double* __restrict__ lu, int L,
-                                            int lane, int2 (&m)[kChunk], double (&v)[kChunk]) {
+// Stream metadata, packed to 32 bits per entry: (position << 16) | slot, slot
+// bit 15 marking a multiplier, slot 0x7fff padding. A chunk is four uint4.
+struct Meta {
+  uint4 q[kChunk / 4];
+};
+
+__device__ __forceinline__ void meta_load(const uint32_t* __restrict__ m, Meta& out) {
 #pragma unroll
-  for (int s = 0; s < kChunk; s += 2) {
-    const int4 mm = __ldg(reinterpret_cast<const int4*>(meta + s));
-    m[s] = make_int2(mm.x, mm.y);
-    m[s + 1] = make_int2(mm.z, mm.w);
-  }
+  for (int i = 0; i < kChunk / 4; ++i) out.q[i] = __ldg(reinterpret_cast<const uint4*>(m) + i);
+}
+
+__device__ __forceinline__ uint32_t meta_at(const Meta& m, int s) {
+  const uint4 v = m.q[s >> 2];
+  return (s & 3) == 0 ? v.x : (s & 3) == 1 ? v.y : (s & 3) == 2 ? v.z : v.w;
+}
+
+// Copy the chunk's 16 operands of this lane (U entries of finished rows or
+// pivot reciprocals; padding copies entry 0) into the ring slot.
+__device__ __forceinline__ void ring_issue(const Meta& m, const double* __restrict__ lu, int L, int lane,
+                                           double* ring_slot) {
+  const unsigned dst0 = (unsigned)__cvta_generic_to_shared(ring_slot + lane);
 #pragma unroll
   for (int s = 0; s < kChunk; ++s) {
-    const int x = m[s].x;
-    const int pos = x >= 0 ? x : -1 - x;
-    v[s] = lu[(int64_t)pos * L + lane];
+    const uint32_t word = meta_at(m, s);
+    const double* g = lu + (int64_t)(word >> 16) * L + lane;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst0 + (unsigned)(s * L * 8)), "l"(g));
   }
 }
 
-__device__ __forceinline__ void stream_compute(const int2 (&m)[kChunk], const double (&v)[kChunk], double* w,
-                                               double* lu, int L, int lane, double& l, int& q) {
+__device__ __forceinline__ void ring_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ void ring_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(kRingChunks - 1) : "memory");
+}
+
+// One hazard-free chunk (symbolic.cpp builds them): read every work-row value
+// the chunk touches, apply the multipliers and updates in order in registers
+// (updates are independent FMAs; only a multiplier starts a new dependency),
+// then write the updated values back.
+__device__ __forceinline__ void ring_compute(const Meta& m, const double* ring_slot, double* w, double* lu, int L,
+                                             int lane, double& l, int& q) {
+  double wv[kChunk];
 #pragma unroll
   for (int s = 0; s < kChunk; ++s) {
-    const int x = m[s].x, y = m[s].y;
-    if (x >= 0) {
-      WROW(y) = fma(-l, v[s], WROW(y));
-    } else if (y >= 0) {
-      l = WROW(y) * v[s];
+    const uint32_t y = meta_at(m, s) & 0x7fffu;
+    wv[s] = y != 0x7fffu ? WROW(y) : 0.0;
+  }
+#pragma unroll
+  for (int s = 0; s < kChunk; ++s) {
+    const uint32_t word = meta_at(m, s);
+    const uint32_t y = word & 0x7fffu;
+    const double v = ring_slot[s * L + lane];
+    if (word & 0x8000u) {
+      l = wv[s] * v;
       SCR(lu, q) = l;
       ++q;
+    } else if (y != 0x7fffu) {
+      wv[s] = fma(-l, v, wv[s]);
     }
+  }
+#pragma unroll
+  for (int s = 0; s < kChunk; ++s) {
+    const uint32_t word = meta_at(m, s);
+    const uint32_t y = word & 0x7fffu;
+    if (!(word & 0x8000u) && y != 0x7fffu) WROW(y) = wv[s];
   }
 }
 
-__device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
-                              double* w, bool alg_only) {
+__device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln, double alpha, const double* negj,
+                                           double* lu, double* w, bool alg_only) {
   const int L = ln.L, lane = ln.lane;
   const int n = p.t.n;
   const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
   const int32_t* __restrict__ diag = p.t.lu_diag;
-  const int32_t* __restrict__ col = p.t.lu_col;
+  double* ring = w + (int64_t)p.t.max_row_len * L;
   for (int r = 0; r < n; ++r) {
     const int q0 = __ldg(rowp + r), q1 = __ldg(rowp + r + 1), dg = __ldg(diag + r);
-    assemble_row(p, ln, r, q0, q1, alpha, negj, w, alg_only);
-    const int t0 = __ldg(p.t.el_ptr + r), t1 = __ldg(p.t.el_ptr + r + 1);
+    // assemble row r of alpha*M - J into the compressed work row
+    for (int s = 0; s < q1 - q0; ++s) WROW(s) = 0.0;
+    const double mr = __ldg(p.t.mass + r);
+    if (!alg_only || mr == 0.0) {
+      const int e1 = __ldg(p.t.j_row_ptr + r + 1);
+      for (int e = __ldg(p.t.j_row_ptr + r); e < e1; ++e) WROW(__ldg(p.t.j_pos + e) - q0) = SCR(negj, e);
+    }
+    WROW(dg - q0) = __dadd_rn(WROW(dg - q0), __dmul_rn(alpha, mr));
+    const int t0 = __ldg(p.t.el_ptr + r);
+    const int nch = (__ldg(p.t.el_ptr + r + 1) - t0) / kChunk;
+    const uint32_t* meta = p.t.elp + t0;
     double l = 0.0;
     int q = q0;
-    if (t1 > t0) {
-      int2 mA[kChunk], mB[kChunk];
-      double vA[kChunk], vB[kChunk];
-      stream_load(p.t.el + t0, lu, L, lane, mA, vA);
-      int t = t0;
-      for (;;) {
-        const bool more = t + kChunk < t1;
-        if (more) stream_load(p.t.el + t + kChunk, lu, L, lane, mB, vB);
-        stream_compute(mA, vA, w, lu, L, lane, l, q);
-        t += kChunk;
-        if (!more) break;
-        const bool more2 = t + kChunk < t1;
-        if (more2) stream_load(p.t.el + t + kChunk, lu, L, lane, mA, vA);
-        stream_compute(mB, vB, w, lu, L, lane, l, q);
-        t += kChunk;
-        if (!more2) break;
+    Meta mi, mc;
+#pragma unroll 1
+    for (int c = 0; c < kRingChunks - 1; ++c) {
+      if (c < nch) {
+        meta_load(meta + c * kChunk, mi);
+        ring_issue(mi, lu, L, lane, ring + (int64_t)(c % kRingChunks) * kChunk * L);
       }
+      ring_commit();
     }
-    SCR(lu, dg) = 1.0 / WROW(r);
-    for (int qq = dg + 1; qq < q1; ++qq) SCR(lu, qq) = WROW(__ldg(col + qq));
+    if (kRingChunks - 1 < nch) meta_load(meta + (kRingChunks - 1) * kChunk, mi);
+    if (nch > 0) meta_load(meta, mc);
+#pragma unroll 1
+    for (int c = 0; c < nch; ++c) {
+      const int ahead = c + kRingChunks - 1;
+      Meta mi_next, mc_next;
+      if (ahead + 1 < nch) meta_load(meta + (ahead + 1) * kChunk, mi_next);
+      if (c + 1 < nch) meta_load(meta + (c + 1) * kChunk, mc_next);
+      if (ahead < nch) ring_issue(mi, lu, L, lane, ring + (int64_t)(ahead % kRingChunks) * kChunk * L);
+      ring_commit();
+      ring_wait();
+      ring_compute(mc, ring + (int64_t)(c % kRingChunks) * kChunk * L, w, lu, L, lane, l, q);
+      mi = mi_next;
+      mc = mc_next;
+    }
+    SCR(lu, dg) = 1.0 / WROW(dg - q0);
+    for (int qq = dg + 1; qq < q1; ++qq) SCR(lu, qq) = WROW(qq - q0);
   }
 }
 
-// Forward and backward substitution with the factor entries of a row loaded
-// eight at a time ahead of their use, two partial sums per row.
-__device__ void lu_solve_pipelined(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
-  const int L = ln.L, lane = ln.lane;
-  const int n = p.t.n;
-  const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
-  const int32_t* __restrict__ diag = p.t.lu_diag;
-  const int32_t* __restrict__ col = p.t.lu_col;
-  for (int r = 0; r < n; ++r) {
-    double a0 = WROW(r), a1 = 0.0;
-    int q = __ldg(rowp + r);
-    const int dg = __ldg(diag + r);
-    for (; q + 7 < dg; q += 8) {
-      double v[8];
-      int c[8];
+// Forward and backward substitution driven by the solve streams
+// (symbolic.h): the factor entries are loaded one chunk ahead of their use
+// (they do not depend on the solution), the solution entries are read from
+// shared memory when the chunk computes.
+__device__ __forceinline__ void solve_load(const int2* __restrict__ meta, const double* __restrict__ lu, int L,
+                                           int lane, int4 (&m)[kChunk / 2], double (&v)[kChunk]) {
 #pragma unroll
-      for (int s = 0; s < 8; ++s) {
-        v[s] = SCR(lu, q + s);
-        c[s] = __ldg(col + q + s);
-      }
+  for (int s = 0; s < kChunk / 2; ++s) m[s] = __ldg(reinterpret_cast<const int4*>(meta) + s);
 #pragma unroll
-      for (int s = 0; s < 8; s += 2) {
-        a0 = fma(-v[s], WROW(c[s]), a0);
-        a1 = fma(-v[s + 1], WROW(c[s + 1]), a1);
-      }
-    }
-    for (; q < dg; ++q) a0 = fma(-SCR(lu, q), WROW(__ldg(col + q)), a0);
-    WROW(r) = a0 + a1;
+  for (int s = 0; s < kChunk / 2; ++s) {
+    const int p0 = m[s].x >= 0 ? m[s].x : -1 - m[s].x;
+    const int p1 = m[s].z >= 0 ? m[s].z : -1 - m[s].z;
+    v[2 * s] = lu[(int64_t)p0 * L + lane];
+    v[2 * s + 1] = lu[(int64_t)p1 * L + lane];
   }
-  for (int r = n - 1; r >= 0; --r) {
-    double a0 = WROW(r), a1 = 0.0;
-    const int dg = __ldg(diag + r), q1 = __ldg(rowp + r + 1);
-    const double dinv = SCR(lu, dg);
-    int q = dg + 1;
-    for (; q + 7 < q1; q += 8) {
-      double v[8];
-      int c[8];
-#pragma unroll
-      for (int s = 0; s < 8; ++s) {
-        v[s] = SCR(lu, q + s);
-        c[s] = __ldg(col + q + s);
-      }
-#pragma unroll
-      for (int s = 0; s < 8; s += 2) {
-        a0 = fma(-v[s], WROW(c[s]), a0);
-        a1 = fma(-v[s + 1], WROW(c[s + 1]), a1);
-      }
-    }
-    for (; q < q1; ++q) a0 = fma(-SCR(lu, q), WROW(__ldg(col + q)), a0);
-    WROW(r) = (a0 + a1) * dinv;
+}
+
+// Four partial sums per row, entry s of a chunk feeding sum s mod 4: the
+// row's FMAs form four independent chains instead of one, so FP64 latency
+// overlaps.
+template <bool kBackward>
+__device__ __forceinline__ void solve_entry(int s, int y, double v, double* w, int L, int lane, double (&acc)[4]) {
+  if (y >= 0) {
+    acc[s & 3] = fma(-v, WROW(y), acc[s & 3]);
+  } else if (y != kNoop) {
+    const int r = -1 - y;
+    const double b = WROW(r) + ((acc[0] + acc[1]) + (acc[2] + acc[3]));
+    WROW(r) = kBackward ? b * v : b;
+    acc[0] = acc[1] = acc[2] = acc[3] = 0.0;
   }
+}
+
+template <bool kBackward>
+__device__ __forceinline__ void solve_compute(const int4 (&m)[kChunk / 2], const double (&v)[kChunk], double* w,
+                                              int L, int lane, double (&acc)[4]) {
+#pragma unroll
+  for (int s = 0; s < kChunk / 2; ++s) {
+    solve_entry<kBackward>(2 * s, m[s].y, v[2 * s], w, L, lane, acc);
+    solve_entry<kBackward>(2 * s + 1, m[s].w, v[2 * s + 1], w, L, lane, acc);
+  }
+}
+
+template <bool kBackward>
+__device__ void solve_stream(const int2* __restrict__ st, int nst, const double* lu, double* w, int L, int lane) {
+  int4 mA[kChunk / 2], mB[kChunk / 2];
+  double vA[kChunk], vB[kChunk];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const int nch = nst / kChunk;
+  solve_load(st, lu, L, lane, mA, vA);
+#pragma unroll 1
+  for (int c = 0; c < nch; c += 2) {
+    if (c + 1 < nch) solve_load(st + (c + 1) * kChunk, lu, L, lane, mB, vB);
+    solve_compute<kBackward>(mA, vA, w, L, lane, acc);
+    if (c + 1 >= nch) break;
+    if (c + 2 < nch) solve_load(st + (c + 2) * kChunk, lu, L, lane, mA, vA);
+    solve_compute<kBackward>(mB, vB, w, L, lane, acc);
+  }
+}
+
+__device__ __noinline__ void lu_solve_pipelined(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
+  solve_stream<false>(p.t.sf, p.t.nsf, lu, w, ln.L, ln.lane);
+  solve_stream<true>(p.t.sb, p.t.nsb, lu, w, ln.L, ln.lane);
 }
 
 // Forward and backward substitution in place on w (fastode/linalg.py:80-81).
@@ -363,7 +430,7 @@ __device__ double block_sum(double v, double* red) {
 
 // One attempt's stages (fastode/solvers.py:54-86), then Y_new, the error
 // estimate and this lane's share of the error norm (fastode/solvers.py:37-43).
-__device__ double attempt(const SolveParams& p, const Lane& ln, double H, const double* Y, double* Ynew,
+__device__ __noinline__ double attempt(const SolveParams& p, const Lane& ln, double H, const double* Y, double* Ynew,
                           double* scr, double* w, long long& c_rhs, long long& c_solves) {
   const int L = ln.L, lane = ln.lane;
   const int n = p.t.n;
@@ -821,6 +888,46 @@ cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream
     configured_smem = (int)smem;
   }
   solve_kernel<<<grid, p.lanes, smem, stream>>>(p);
+  return cudaGetLastError();
+}
+
+// Several mechanisms in one persistent launch: the batch table lives in the
+// workspace, items [starts[b], starts[b+1]) of the queue are the groups of
+// batch b, and each block integrates whatever group it pulls next.
+__global__ void __launch_bounds__(256) solve_multi_kernel(const SolveParams* __restrict__ batches, int nb,
+                                                          const int32_t* __restrict__ starts, int32_t* queue,
+                                                          double* scratch, int64_t slot_doubles) {
+  extern __shared__ double smem[];
+  double* red = smem;
+  double* w = smem + 32;
+  double* scr = scratch + (int64_t)blockIdx.x * slot_doubles;
+  __shared__ int next;
+  const int total = starts[nb];
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) next = atomicAdd(queue, 1);
+    __syncthreads();
+    const int item = next;
+    if (item >= total) break;
+    int b = 0;
+    while (b + 1 < nb && item >= starts[b + 1]) ++b;
+    solve_group(batches[b], item - starts[b], scr, w, red);
+  }
+}
+
+cudaError_t launch_solve_multi(const SolveParams* batches, int nb, const int32_t* starts, int32_t* queue,
+                               double* scratch, int64_t slot_doubles, int grid, int lanes, size_t smem,
+                               cudaStream_t stream) {
+  static int configured_smem = -1;
+  if ((int)smem > 48 * 1024 && (int)smem != configured_smem) {
+    cudaError_t e =
+        cudaFuncSetAttribute(solve_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured_smem = (int)smem;
+  }
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int32_t), stream);
+  if (e != cudaSuccess) return e;
+  solve_multi_kernel<<<grid, lanes, smem, stream>>>(batches, nb, starts, queue, scratch, slot_doubles);
   return cudaGetLastError();
 }
 

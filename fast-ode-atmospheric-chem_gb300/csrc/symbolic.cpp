@@ -275,26 +275,86 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
     t->lu_row_ptr.push_back((int32_t)t->lu_col.size());
   }
 
-  // elimination stream, row by row, each row padded to whole chunks
+  // elimination stream, row by row, each row padded to whole chunks; the
+  // targets are slots of the row's own pattern (its position minus the row
+  // start), so the work row needs max_row_len entries, not n
   t->el_ptr.assign(1, 0);
   t->el.clear();
+  t->max_row_len = 0;
+  // Every chunk is hazard-free: no slot is updated twice in it and no
+  // multiplier reads a slot an earlier entry of the same chunk updated. The
+  // device can then read a chunk's work-row values at once, run its updates as
+  // independent FMAs (only the multipliers chain them) and write back: FP64
+  // latency overlaps instead of serializing every read-modify-write.
+  std::vector<int> slot_of(n, -1);
+  std::vector<int64_t> touched(n, -1);  // absolute chunk that last updated a slot
+  auto entries = [&]() { return (int64_t)(t->el.size() / 2); };
+  auto pad = [&]() {
+    while (entries() % kStreamChunk != 0) {
+      t->el.push_back(-1);
+      t->el.push_back(-1);
+    }
+  };
   for (int r = 0; r < n; ++r) {
-    size_t start = t->el.size();
-    for (int q = t->lu_row_ptr[r]; q < t->lu_diag[r]; ++q) {
+    const int q0 = t->lu_row_ptr[r];
+    t->max_row_len = std::max(t->max_row_len, t->lu_row_ptr[r + 1] - q0);
+    for (int q = q0; q < t->lu_row_ptr[r + 1]; ++q) slot_of[t->lu_col[q]] = q - q0;
+    for (int q = q0; q < t->lu_diag[r]; ++q) {
       const int k = t->lu_col[q];
+      const int ym = q - q0;                        // the multiplier reads slot ym
+      if (touched[ym] == entries() / kStreamChunk) pad();
       t->el.push_back(-1 - t->lu_diag[k]);
-      t->el.push_back(k);
+      t->el.push_back(ym);
       for (int u = t->lu_diag[k] + 1; u < t->lu_row_ptr[k + 1]; ++u) {
+        const int y = slot_of[t->lu_col[u]];
+        if (touched[y] == entries() / kStreamChunk) pad();
+        touched[y] = entries() / kStreamChunk;
         t->el.push_back(u);
-        t->el.push_back(t->lu_col[u]);
+        t->el.push_back(y);
       }
     }
-    while (((t->el.size() - start) / 2) % kStreamChunk != 0) {
-      t->el.push_back(-1);
-      t->el.push_back(-1);
-    }
+    pad();
     t->el_ptr.push_back((int32_t)(t->el.size() / 2));
   }
+
+  // packed copy of the elimination stream
+  t->elp.clear();
+  if ((int64_t)t->lu_col.size() <= 65536 && t->max_row_len < 0x7fff) {
+    t->elp.reserve(t->el.size() / 2);
+    for (size_t e = 0; e < t->el.size(); e += 2) {
+      const int32_t x = t->el[e], y = t->el[e + 1];
+      uint32_t word;
+      if (x >= 0) word = ((uint32_t)x << 16) | (uint32_t)y;                       // update
+      else if (y >= 0) word = ((uint32_t)(-1 - x) << 16) | 0x8000u | (uint32_t)y;  // multiplier
+      else word = 0x7fffu;                                                        // padding
+      t->elp.push_back(word);
+    }
+  }
+
+  // triangular-solve streams (one flat sequence each, padded at the end)
+  t->sf.clear();
+  t->sb.clear();
+  for (int r = 0; r < n; ++r) {
+    for (int q = t->lu_row_ptr[r]; q < t->lu_diag[r]; ++q) {
+      t->sf.push_back(q);
+      t->sf.push_back(t->lu_col[q]);
+    }
+    t->sf.push_back(-1);
+    t->sf.push_back(-1 - r);
+  }
+  for (int r = n - 1; r >= 0; --r) {
+    for (int q = t->lu_diag[r] + 1; q < t->lu_row_ptr[r + 1]; ++q) {
+      t->sb.push_back(q);
+      t->sb.push_back(t->lu_col[q]);
+    }
+    t->sb.push_back(-1 - t->lu_diag[r]);
+    t->sb.push_back(-1 - r);
+  }
+  for (std::vector<int32_t>* s : {&t->sf, &t->sb})
+    while ((s->size() / 2) % kStreamChunk != 0) {
+      s->push_back(-1);
+      s->push_back(kNoop);
+    }
 
   // Jacobian entries in assembly order
   std::vector<std::vector<std::pair<int, int>>> by_row(n);  // (perm col, original entry)

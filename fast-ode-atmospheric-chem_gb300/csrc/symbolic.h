@@ -8,11 +8,10 @@
 #include <vector>
 
 #include "fastode_gb300.h"
+#include "stream.h"
 
 namespace fo {
 
-// Entries per software-pipelined chunk of the elimination stream.
-constexpr int kStreamChunk = 16;
 
 // Everything the device needs, in the permuted species numbering
 // (p = 0..n-1 is the p-th eliminated species, perm[p] its original index).
@@ -45,10 +44,25 @@ struct HostTables {
   // Elimination stream: for row r, entries el[2*t], el[2*t+1] for
   // el_ptr[r] <= t < el_ptr[r+1], padded to a multiple of kStreamChunk.
   //   update  (x >= 0):          w[y] -= l * lu[x]    (x: a U entry of an earlier row)
-  //   marker  (x < 0, y >= 0):   l = w[y] * lu[-1-x]  (y = k, -1-x = diagonal slot of row k,
-  //                              which holds 1/pivot); l is stored in the next L slot of row r
+  //   marker  (x < 0, y >= 0):   l = w[y] * lu[-1-x]  (-1-x = diagonal slot of row k, which
+  //                              holds 1/pivot); l is stored in the next L slot of row r
   //   no-op   (x = -1, y = -1):  padding
+  // y is a slot of row r's own pattern: w[y] stands for lu[lu_row_ptr[r] + y].
   std::vector<int32_t> el_ptr, el;
+  int max_row_len = 0;
+  // The same stream packed to 32 bits per entry, (position << 16) | slot,
+  // slot bit 15 set for a multiplier, slot 0x7fff for padding; empty when a
+  // position or a slot does not fit (the plain kernel then runs instead).
+  std::vector<uint32_t> elp;
+
+  // Triangular-solve streams (entries (x, y), padded to whole chunks):
+  // forward over rows 0..n-1, backward over rows n-1..0.
+  //   update (y >= 0):              acc -= lu[x] * v[y]
+  //   row end (y < 0, y != kNoop):  r = -1 - y; v[r] = v[r] + acc (forward) or
+  //                                 (v[r] + acc) * lu[-1-x] (backward, -1-x = diagonal
+  //                                 slot holding 1/pivot); acc = 0
+  //   no-op (y == kNoop)
+  std::vector<int32_t> sf, sb;
 
   int64_t lu_fma = 0, solve_fma = 0;
   int nnz_l = 0, nnz_u = 0;

@@ -41,6 +41,20 @@ __global__ void photolysis_kernel(int C, int nphoto, const int32_t* __restrict__
   k[(int64_t)c * kcs + (int64_t)rxn[p] * krs] = J[p] * (f > 0.0 ? f : 0.0);
 }
 
+__global__ void photolysis_clock_kernel(int C, int nphoto, const int32_t* __restrict__ rxn,
+                                        const double* __restrict__ J, const double* __restrict__ phase, double omega,
+                                        const double* __restrict__ t_dev, double* __restrict__ k, int64_t kcs,
+                                        int64_t krs) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)C * nphoto) return;
+  const int c = (int)(idx % C);
+  const int p = (int)(idx / C);
+  const double f = cos(phase[c] + omega * t_dev[0]);
+  k[(int64_t)c * kcs + (int64_t)rxn[p] * krs] = J[p] * (f > 0.0 ? f : 0.0);
+}
+
+__global__ void advance_clock_kernel(double* t_dev, double dt) { t_dev[0] += dt; }
+
 // Eight independent FMA chains per thread; every warp is full.
 __global__ void fma_rate_kernel(double* out, int iters) {
   double a0 = 0.5, a1 = 1.0, a2 = 1.5, a3 = 2.0, a4 = 2.5, a5 = 3.0, a6 = 3.5, a7 = 4.0;
@@ -78,6 +92,24 @@ int fo_update_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const do
   const int block = 256;
   photolysis_kernel<<<(unsigned)((total + block - 1) / block), block, 0, (cudaStream_t)stream>>>(
       C, nphoto, rxn, J, phase, omega * t, k, k_cell_stride, k_reaction_stride);
+  return cudaGetLastError() == cudaSuccess ? FO_OK : FO_E_CUDA;
+}
+
+int fo_update_photolysis_clock(int32_t C, int32_t nphoto, const int32_t* rxn, const double* J, const double* phase,
+                               double omega, const double* t_dev, double* k, int64_t k_cell_stride,
+                               int64_t k_reaction_stride, void* stream) {
+  if (C < 0 || nphoto < 0 || !t_dev || (nphoto > 0 && (!rxn || !J || !phase || !k))) return FO_E_INVALID;
+  const int64_t total = (int64_t)C * nphoto;
+  if (total == 0) return FO_OK;
+  const int block = 256;
+  photolysis_clock_kernel<<<(unsigned)((total + block - 1) / block), block, 0, (cudaStream_t)stream>>>(
+      C, nphoto, rxn, J, phase, omega, t_dev, k, k_cell_stride, k_reaction_stride);
+  return cudaGetLastError() == cudaSuccess ? FO_OK : FO_E_CUDA;
+}
+
+int fo_advance_clock(double* t_dev, double dt, void* stream) {
+  if (!t_dev) return FO_E_INVALID;
+  advance_clock_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(t_dev, dt);
   return cudaGetLastError() == cudaSuccess ? FO_OK : FO_E_CUDA;
 }
 

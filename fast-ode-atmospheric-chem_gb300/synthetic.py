@@ -164,6 +164,23 @@ def plain_small(n_cells: int = 64, intervals: int = 20, seed: int = 1) -> Worklo
     return Workload("ros3-20x40", sm, cells, 30.0, intervals, 1.0e-3, 32, False)
 
 
+def batched_uneven(n_cells: int = 1_048_576, intervals: int = 240, seed: int = 3,
+                   sizes=((60, 40), (120, 260), (210, 500))) -> list:
+    """Batched uneven workload: the cells split (in whole groups of 32) across
+    three synthetic mechanisms, T U[200, 310] K, p U[10, 1000] hPa, a solar
+    phase U(-pi, pi) so that half the cells are in darkness (J = 0), dt = 60 s,
+    rtol 1e-3, photolysis updated at every interval start."""
+    groups = n_cells // 32
+    share = [groups // len(sizes) + (1 if i < groups % len(sizes) else 0) for i in range(len(sizes))]
+    out = []
+    for i, ((n, R), g) in enumerate(zip(sizes, share)):
+        sm = synthetic_mechanism(n, R, seed + 10 * i, third_body_fraction=0.1)
+        cells = synthetic_cells(sm, g * 32, seed + 10 * i + 1000, T_range=(200.0, 310.0),
+                                p_range_hpa=(10.0, 1000.0), phase_range=(-math.pi, math.pi))
+        out.append(Workload(f"ros3-{n}x{R}", sm, cells, 60.0, intervals, 1.0e-3, 32, True))
+    return out
+
+
 def plain_large(n_cells: int = 65536, intervals: int = 120, seed: int = 2) -> Workload:
     """Plain ROS3, 210 species / 500 reactions, 65,536 cells in groups of 32,
     T U[200, 310] K, p U[10, 1000] hPa setting [M], dt = 30 s x 120 intervals,

@@ -1,0 +1,99 @@
+"""Autotuner: choose the kernel variant, the group size and the launch shape
+per mechanism by measuring them on a sample of the workload.
+
+Group size is a numerical choice as well as a speed one: the cells of a group
+share one step sequence and one error norm (the reference's groups of 32,
+fastode/ts1.py:196), so a larger group takes the steps its stiffest cell needs
+and a smaller one wastes lanes of a warp (a warp of 32 lanes costs the same
+FP64 issue slots however many lanes hold cells). The tuner therefore scores
+candidates by cell-intervals per second on the sample, which counts both.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SMEM_LIMIT = 232448
+
+
+@dataclass(frozen=True)
+class Config:
+    kernel: str = "pipelined"     # FO_VARIANT_*
+    group_size: int = 32
+    persistent: bool = False      # one block per group, or persistent blocks pulling a queue
+
+
+@dataclass
+class TuneResult:
+    best: Config
+    table: list = field(default_factory=list)   # (config, cell-intervals/s or None when it does not fit)
+
+
+def fits(smem_doubles_per_cell: int, group_size: int) -> bool:
+    lanes = ((group_size + 31) // 32) * 32
+    return 8 * (32 + smem_doubles_per_cell * lanes) <= SMEM_LIMIT
+
+
+def candidates(smem_doubles_per_cell: int, group_sizes=(16, 32, 64, 128),
+               kernels=("pipelined", "plain"), persistent=(False, True)) -> list:
+    out = []
+    for k in kernels:
+        for g in group_sizes:
+            for p in persistent:
+                out.append(Config(k, g, p))
+    return out
+
+
+def autotune(measure, smem_doubles_per_cell: int, configs=None) -> TuneResult:
+    """measure(config) -> cell-intervals/s; configs that do not fit in shared
+    memory are skipped (scored None). Returns the fastest."""
+    configs = configs if configs is not None else candidates(smem_doubles_per_cell)
+    table = []
+    best, best_v = None, -1.0
+    for c in configs:
+        if not fits(smem_doubles_per_cell, c.group_size):
+            table.append((c, None))
+            continue
+        v = float(measure(c))
+        table.append((c, v))
+        if v > best_v:
+            best, best_v = c, v
+    if best is None:
+        raise ValueError("no candidate configuration fits in shared memory")
+    return TuneResult(best, table)
+
+
+def measure_on_device(mech, Y0, k_of, dt, atol, rtol, warm: int = 1, timed: int = 2, mass=None):
+    """A measure function for ``autotune``: integrates the sample cells Y0
+    (C, n) with each configuration over `warm` untimed and `timed` timed
+    intervals (k_of(i) -> (C, R) host rate constants) and returns
+    cell-intervals per second of the timed intervals."""
+    import torch
+
+    from .batch import Batch
+    from .multi import default_slots
+    from .solvers import Algorithm
+
+    ks = [torch.from_numpy(np.ascontiguousarray(k_of(i).T)).cuda() for i in range(warm + timed)]
+    at = torch.from_numpy(np.ascontiguousarray(atol, dtype=np.float64)).cuda()
+
+    def measure(c: Config) -> float:
+        alg = Algorithm(kernel=c.kernel)
+        b = Batch(mech, Y0, group_size=c.group_size, algorithm=alg, mass=mass)
+        if c.persistent:
+            lanes = ((c.group_size + 31) // 32) * 32
+            per_sm = max(1, min(8, SMEM_LIMIT // (8 * (32 + b.plan.info["smem_doubles_per_cell"] * lanes))))
+            b = Batch(mech, Y0, group_size=c.group_size, algorithm=alg, mass=mass,
+                      slots=torch.cuda.get_device_properties(b.plan.device).multi_processor_count * per_sm)
+        for i in range(warm):
+            b.step(ks[i], dt, at, rtol)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(warm, warm + timed):
+            b.step(ks[i], dt, at, rtol)
+        torch.cuda.synchronize()
+        return b.C * timed / (time.perf_counter() - t0)
+
+    return measure

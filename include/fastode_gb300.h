@@ -183,6 +183,54 @@ int fo_solve(const fo_plan* plan, const fo_options* opt,
              double* trace, int32_t trace_cap, int32_t* trace_len,
              void* stream);
 
+/*
+ * Several mechanisms in one persistent launch. Each batch is what one
+ * fo_solve call takes (a plan, its options and groups, its state, rate
+ * constants, tolerances, memory, counters and statuses, all device
+ * pointers); the launch's blocks pull groups of every batch from one device
+ * queue, largest mechanisms first. The device form of running the reference's
+ * scenario loop (fastode/ts1.py:196-222) over several mechanisms at once.
+ *
+ * fo_multi_prepare validates the batches, checks the workspace (see
+ * fo_multi_workspace_bytes) and writes the batch table into it (synchronous);
+ * fo_multi_launch then only resets the queue and launches, so it can be
+ * captured in a CUDA graph and replayed once per interval. The pointers given
+ * to prepare must stay valid for every launch.
+ */
+typedef struct fo_batch_desc {
+  const fo_plan* plan;
+  fo_options opt;
+  int32_t ngroups;
+  const int32_t* group_offsets;   /* device, ngroups+1 */
+  int32_t max_group_cells;        /* 1..256 */
+  double* Y;
+  int64_t y_cell_stride, y_species_stride;
+  const double* k;
+  int64_t k_cell_stride, k_reaction_stride;
+  const double* atol;
+  double rtol, dt;
+  double* memory;
+  int64_t* counts;
+  int32_t* status;
+} fo_batch_desc;
+
+typedef struct fo_multi fo_multi;  /* opaque */
+
+int fo_multi_workspace_bytes(int32_t nbatches, const fo_batch_desc* batches, int32_t slots, size_t* bytes);
+int fo_multi_prepare(int32_t nbatches, const fo_batch_desc* batches, void* workspace, size_t workspace_bytes,
+                     int32_t slots, fo_multi** multi);
+int fo_multi_launch(const fo_multi* multi, void* stream);
+int fo_multi_destroy(fo_multi* multi);
+
+/* Photolysis update reading the time from device memory (t_dev, one double),
+ * and a clock advance t_dev += dt: together they make an interval's launches
+ * independent of the interval index, so one captured CUDA graph serves every
+ * interval (fastode/ts1.py:204 evaluates the factor at the interval start). */
+int fo_update_photolysis_clock(int32_t C, int32_t nphoto, const int32_t* rxn, const double* J,
+                               const double* phase, double omega, const double* t_dev, double* k,
+                               int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
+int fo_advance_clock(double* t_dev, double dt, void* stream);
+
 /* Forcing F(Y) (C x n, written with the Y strides into F) for C cells:
  * fastode.chem.Mechanism.rhs (fastode/chem.py:89-90). Device pointers. */
 int fo_eval_rhs(const fo_plan* plan, int32_t C,

@@ -1,0 +1,40 @@
+"""The autotuner's host logic (CPU): candidates, shared-memory fit, choice."""
+import pytest
+
+from fastode_gb300.tune import Config, autotune, candidates, fits
+
+
+def test_fits_follows_shared_memory():
+    # 210 species: 4 warps of 32 lanes fit (217 KB), 8 do not
+    assert fits(210, 32) and fits(210, 128)
+    assert not fits(210, 256)
+    assert fits(20, 256)
+
+
+def test_autotune_picks_the_fastest_that_fits():
+    speed = {("pipelined", 32, False): 10.0, ("pipelined", 64, True): 12.0, ("plain", 32, False): 5.0}
+
+    def measure(c):
+        return speed.get((c.kernel, c.group_size, c.persistent), 1.0)
+
+    r = autotune(measure, 210)
+    assert r.best == Config("pipelined", 64, True)
+    assert len(r.table) == len(candidates(210))
+
+
+def test_autotune_skips_configs_that_do_not_fit():
+    calls = []
+
+    def measure(c):
+        calls.append(c)
+        return float(c.group_size)
+
+    r = autotune(measure, 400, [Config("pipelined", 32), Config("pipelined", 128)])
+    assert r.best == Config("pipelined", 32)
+    assert [c for c, v in r.table if v is None] == [Config("pipelined", 128)]
+    assert calls == [Config("pipelined", 32)]
+
+
+def test_autotune_raises_when_nothing_fits():
+    with pytest.raises(ValueError):
+        autotune(lambda c: 1.0, 5000, [Config("pipelined", 64)])
