@@ -89,6 +89,12 @@ SIGNATURES = {
     "fo_multi_destroy": (C.c_int, [_P]),
     "fo_update_photolysis_clock": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _P, _P, _I64, _I64, _P]),
     "fo_advance_clock": (C.c_int, [_P, _D, _P]),
+    "fo_adjoint_workspace_bytes": (C.c_int, [_P, _I32, _I32, _I32, C.POINTER(C.c_size_t)]),
+    "fo_adjoint_interval": (C.c_int, [_P, C.POINTER(Options), _I32, _P, _I32,
+                                      _P, _I64, _I64, _P, _I64, _I64, _P, _D,
+                                      _P, _P, _I32, _I32,
+                                      _P, _I64, _I64, _P, _I64, _I64, _P, _I64, _I64,
+                                      _P, _P, C.c_size_t, _P]),
 }
 
 _lib = None

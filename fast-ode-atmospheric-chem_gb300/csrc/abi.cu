@@ -17,6 +17,7 @@
 namespace fo {
 cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream);
 cudaError_t launch_eval(const SolveParams& p, int C, int want_jac, double* out, cudaStream_t stream);
+cudaError_t launch_adjoint(const AdjParams& a, int grid, int lanes, size_t smem, cudaStream_t stream);
 cudaError_t launch_solve_multi(const SolveParams* batches, int nb, const int32_t* starts, int32_t* queue,
                                double* scratch, int64_t slot_doubles, int grid, int lanes, size_t smem,
                                cudaStream_t stream);
@@ -176,7 +177,8 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
          o_jtp = append(buf, t.jt_ptr), o_jti = append(buf, t.jt_idx), o_jtv = append(buf, t.jt_val),
          o_lur = append(buf, t.lu_row_ptr), o_lud = append(buf, t.lu_diag), o_luc = append(buf, t.lu_col),
          o_elp = append(buf, t.el_ptr), o_el = append(buf, t.el), o_sf = append(buf, t.sf),
-         o_sb = append(buf, t.sb), o_jpos = append(buf, t.j_lu_pos), o_elpk = append(buf, t.elp);
+         o_sb = append(buf, t.sb), o_jpos = append(buf, t.j_lu_pos), o_elpk = append(buf, t.elp),
+         o_stp = append(buf, t.st_ptr), o_sts = append(buf, t.st_sp), o_stv = append(buf, t.st_val);
   cudaError_t e = cudaGetDevice(&plan->device);
   if (e != cudaSuccess) {
     delete plan;
@@ -218,6 +220,9 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
   d.el_ptr = reinterpret_cast<const int32_t*>(b + o_elp);
   d.el = reinterpret_cast<const int2*>(b + o_el);
   d.elp = t.elp.empty() ? nullptr : reinterpret_cast<const uint32_t*>(b + o_elpk);
+  d.st_ptr = reinterpret_cast<const int32_t*>(b + o_stp);
+  d.st_sp = reinterpret_cast<const int32_t*>(b + o_sts);
+  d.st_val = reinterpret_cast<const double*>(b + o_stv);
   d.sf = reinterpret_cast<const int2*>(b + o_sf);
   d.sb = reinterpret_cast<const int2*>(b + o_sb);
   d.nsf = (int)(t.sf.size() / 2);
@@ -483,6 +488,85 @@ int fo_multi_launch(const fo_multi* m, void* stream) {
 
 int fo_multi_destroy(fo_multi* m) {
   delete m;
+  return FO_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+fo::AdjLayout adjoint_layout(const fo::HostTables& t, int max_steps) {
+  fo::AdjLayout a;
+  int64_t o = layout_of(t).items;
+  a.ys = o; o += (int64_t)max_steps * t.n;
+  a.u = o; o += 4LL * t.n;
+  a.kbar = o; o += 4LL * t.n;
+  a.fbar = o; o += 4LL * t.n;
+  a.ybar = o; o += t.n;
+  a.g = o; o += t.n;
+  a.jbar = o; o += (int64_t)t.j_col.size();
+  a.dbar = o; o += (int64_t)t.R * t.P;
+  a.items = o;
+  return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fo_adjoint_workspace_bytes(const fo_plan* plan, int32_t ngroups, int32_t max_group_cells, int32_t max_steps,
+                               size_t* bytes) {
+  if (!plan || !bytes || ngroups <= 0 || max_group_cells <= 0 || max_steps < 0)
+    return fail(FO_E_INVALID, "bad argument");
+  *bytes = kHeader + sizeof(double) * (size_t)ngroups * (size_t)adjoint_layout(plan->host, max_steps).items *
+                         lanes_for(max_group_cells);
+  return FO_OK;
+}
+
+int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
+                        int32_t max_group_cells, const double* Y, int64_t ycs, int64_t yss, const double* k,
+                        int64_t kcs, int64_t krs, const double* atol, double dt, const int32_t* step_ptr,
+                        const double* steps, int32_t max_steps, int32_t mode, double* lam, int64_t lcs, int64_t lss,
+                        double* thbar, int64_t tcs, int64_t trs, double* Yout, int64_t ocs, int64_t oss,
+                        int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+  if (ngroups <= 0) return FO_OK;
+  if (!Y || !step_ptr || !steps || !status || !workspace) return fail(FO_E_INVALID, "null argument");
+  if (mode != 0 && mode != 1) return fail(FO_E_INVALID, "mode must be 0 (replay) or 1 (adjoint)");
+  if (mode == 0 && !Yout) return fail(FO_E_INVALID, "replay needs Yout");
+  if (mode == 1 && (!lam || !thbar)) return fail(FO_E_INVALID, "adjoint needs lam and thbar");
+  fo::AdjParams a;
+  std::memset(&a, 0, sizeof(a));
+  size_t smem = 0;
+  // the group memory/counters/status of fill_params are not used by the adjoint
+  int rc = fill_params(plan, opt, ngroups, group_offsets, max_group_cells, const_cast<double*>(Y), ycs, yss, k, kcs,
+                       krs, atol, 0.0, dt, reinterpret_cast<double*>(workspace), reinterpret_cast<int64_t*>(workspace),
+                       status, &a.p, &smem);
+  if (rc != FO_OK) return rc;
+  size_t need = 0;
+  fo_adjoint_workspace_bytes(plan, ngroups, max_group_cells, max_steps, &need);
+  if (workspace_bytes < need) return fail(FO_E_WORKSPACE, "workspace too small");
+  a.al = adjoint_layout(plan->host, max_steps);
+  a.p.slot_doubles = a.al.items * a.p.lanes;
+  a.p.scratch = reinterpret_cast<double*>(static_cast<char*>(workspace) + kHeader);
+  a.Ycp = Y;
+  a.ycs = ycs;
+  a.yss = yss;
+  a.lam = lam;
+  a.lcs = lcs;
+  a.lss = lss;
+  a.thbar = thbar;
+  a.tcs = tcs;
+  a.trs = trs;
+  a.Yout = Yout;
+  a.ocs = ocs;
+  a.oss = oss;
+  a.step_ptr = step_ptr;
+  a.steps = steps;
+  a.max_steps = max_steps;
+  a.mode = mode;
+  a.status = status;
+  cudaError_t e = fo::launch_adjoint(a, ngroups, a.p.lanes, smem, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
   return FO_OK;
 }
 

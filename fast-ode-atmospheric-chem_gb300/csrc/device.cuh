@@ -16,6 +16,9 @@ struct DevTables {
   const int32_t* s_ptr;       // n+1
   const int32_t* s_rxn;
   const double* s_val;
+  const int32_t* st_ptr;      // R+1: S by reactions
+  const int32_t* st_sp;       // permuted species
+  const double* st_val;
   const int32_t* j_row_ptr;   // n+1
   const int32_t* j_col;       // nnzj
   const int32_t* j_src;       // nnzj original pattern entry
@@ -81,6 +84,37 @@ struct SolveParams {
   double* trace;
   int trace_cap;
   int32_t* trace_len;
+};
+
+// Extra per-lane scratch of the adjoint (items after the forward layout).
+struct AdjLayout {
+  int64_t ys;     // max_steps * n: state at the start of every step
+  int64_t u;      // 4n: stage points of the stages that evaluate F anew
+  int64_t kbar;   // 4n
+  int64_t fbar;   // 4n
+  int64_t ybar;   // n
+  int64_t g;      // n: a forcing vector-Jacobian product
+  int64_t jbar;   // nnzj
+  int64_t dbar;   // R*P
+  int64_t items;  // total items per lane, forward layout included
+};
+
+struct AdjParams {
+  SolveParams p;        // tables, tableau, forward scratch layout, rate constants, group offsets, dt
+  AdjLayout al;
+  const double* Ycp;    // state at the interval start (checkpoint)
+  int64_t ycs, yss;
+  double* lam;          // in: dL/dY at the interval end; out: dL/dY at the interval start
+  int64_t lcs, lss;
+  double* thbar;        // accumulated dL/dlog k per cell
+  int64_t tcs, trs;
+  double* Yout;         // replay mode: the interval's end state
+  int64_t ocs, oss;
+  const int32_t* step_ptr;  // ngroups+1
+  const double* steps;      // accepted step sizes of the interval
+  int max_steps;
+  int mode;             // 0 replay, 1 adjoint
+  int32_t* status;
 };
 
 }  // namespace fo

@@ -259,6 +259,23 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
     t->s_ptr.push_back((int32_t)t->s_rxn.size());
   }
 
+  // S by reactions (for the adjoint's S^T v)
+  {
+    std::vector<std::vector<std::pair<int, double>>> cols(R);
+    for (int p = 0; p < n; ++p)
+      for (int q = t->s_ptr[p]; q < t->s_ptr[p + 1]; ++q) cols[t->s_rxn[q]].push_back({p, t->s_val[q]});
+    t->st_ptr.assign(1, 0);
+    t->st_sp.clear();
+    t->st_val.clear();
+    for (int j = 0; j < R; ++j) {
+      for (auto& e : cols[j]) {
+        t->st_sp.push_back(e.first);
+        t->st_val.push_back(e.second);
+      }
+      t->st_ptr.push_back((int32_t)t->st_sp.size());
+    }
+  }
+
   // LU structure
   std::vector<std::vector<int>> pat = permuted_pattern(m, t->iperm);
   std::vector<std::vector<int>> rows;
@@ -281,10 +298,12 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
   t->el_ptr.assign(1, 0);
   t->el.clear();
   t->max_row_len = 0;
-  // Every chunk is hazard-free: no slot is updated twice in it and no
-  // multiplier reads a slot an earlier entry of the same chunk updated. The
-  // device can then read a chunk's work-row values at once, run its updates as
-  // independent FMAs (only the multipliers chain them) and write back: FP64
+  // Every chunk is hazard-free over a window of two chunks: no slot is updated
+  // twice in a chunk, and no entry (update or multiplier) touches a slot that
+  // an earlier entry of the same chunk or of the previous chunk updated. The
+  // device then reads a chunk's work-row values at once, runs its updates as
+  // independent FMAs (only the multipliers chain them), and writes them back
+  // only after the next chunk's values are read and its FMAs issued: FP64
   // latency overlaps instead of serializing every read-modify-write.
   std::vector<int> slot_of(n, -1);
   std::vector<int64_t> touched(n, -1);  // absolute chunk that last updated a slot
@@ -295,19 +314,28 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
       t->el.push_back(-1);
     }
   };
+  // close the current chunk (a whole no-op chunk when it is empty)
+  auto pad_chunk = [&]() {
+    t->el.push_back(-1);
+    t->el.push_back(-1);
+    pad();
+  };
   for (int r = 0; r < n; ++r) {
     const int q0 = t->lu_row_ptr[r];
     t->max_row_len = std::max(t->max_row_len, t->lu_row_ptr[r + 1] - q0);
-    for (int q = q0; q < t->lu_row_ptr[r + 1]; ++q) slot_of[t->lu_col[q]] = q - q0;
+    for (int q = q0; q < t->lu_row_ptr[r + 1]; ++q) {
+      slot_of[t->lu_col[q]] = q - q0;
+      touched[q - q0] = -2;                         // the row's slots start unwritten
+    }
     for (int q = q0; q < t->lu_diag[r]; ++q) {
       const int k = t->lu_col[q];
       const int ym = q - q0;                        // the multiplier reads slot ym
-      if (touched[ym] == entries() / kStreamChunk) pad();
+      while (touched[ym] >= entries() / kStreamChunk - 1) pad_chunk();
       t->el.push_back(-1 - t->lu_diag[k]);
       t->el.push_back(ym);
       for (int u = t->lu_diag[k] + 1; u < t->lu_row_ptr[k + 1]; ++u) {
         const int y = slot_of[t->lu_col[u]];
-        if (touched[y] == entries() / kStreamChunk) pad();
+        while (touched[y] >= entries() / kStreamChunk - 1) pad_chunk();
         touched[y] = entries() / kStreamChunk;
         t->el.push_back(u);
         t->el.push_back(y);

@@ -26,6 +26,9 @@ struct HostTables {
   // stoichiometry rows in permuted order: (reaction, coefficient)
   std::vector<int32_t> s_ptr, s_rxn;
   std::vector<double> s_val;
+  // the same by reactions (columns of S): (permuted species, coefficient)
+  std::vector<int32_t> st_ptr, st_sp;
+  std::vector<double> st_val;
 
   // Jacobian values in assembly order (permuted row-major):
   // entry q sits in permuted row r with j_row_ptr[r] <= q < j_row_ptr[r+1],

@@ -181,6 +181,47 @@ def batched_uneven(n_cells: int = 1_048_576, intervals: int = 240, seed: int = 3
     return out
 
 
+@dataclass
+class DaeWorkload(Workload):
+    mass: np.ndarray = None          # (n,) 1 differential, 0 algebraic
+
+
+def dae_constrained(n_cells: int = 16384, intervals: int = 120, seed: int = 5, n_diff: int = 150,
+                    n_alg: int = 10, n_reactions: int = 330) -> DaeWorkload:
+    """RODAS3 constrained workload: a synthetic mechanism of n_diff + n_alg
+    species in which the last n_alg species are held in quasi-steady state
+    (mass = 0, fastode/chem.py:112-113). Each of them gets a fast first-order
+    loss (k = A with A log-uniform on [1e2, 1e4] s^-1, no temperature
+    dependence) into two differential species, so its constraint row has a
+    nonzero diagonal: fast equilibrium with its producers. T U[200, 310] K,
+    p U[10, 1000] hPa, daylight phases U(-1.2, 1.2), dt = 60 s, rtol 1e-4."""
+    n = n_diff + n_alg
+    base = synthetic_mechanism(n, n_reactions, seed, third_body_fraction=0.1)
+    rng = np.random.default_rng(seed + 77)
+    species = base.species
+    reactions = list(base.reactions)
+    A = list(base.A)
+    E = list(base.E)
+    J = list(base.J)
+    photo = list(base.photolytic)
+    for a in range(n_diff, n):
+        prods = rng.integers(0, n_diff, size=2)
+        reactions.append(([species[a]], [(species[int(p)], 1.0) for p in prods]))
+        A.append(10.0 ** rng.uniform(2.0, 4.0))
+        E.append(0.0)
+        J.append(0.0)
+        photo.append(False)
+    mech = Mechanism(species, reactions)
+    sm = SyntheticMechanism(mech, species, reactions, np.array(A), np.array(E), np.array(J),
+                            np.array(photo, dtype=bool))
+    cells = synthetic_cells(sm, n_cells, seed + 1000, T_range=(200.0, 310.0), p_range_hpa=(10.0, 1000.0),
+                            phase_range=(-1.2, 1.2))
+    mass = np.ones(n)
+    mass[n_diff:] = 0.0
+    return DaeWorkload("rodas3-dae-%dx%d" % (n, len(reactions)), sm, cells, 60.0, intervals, 1.0e-4, 32, True,
+                       mass=mass)
+
+
 def plain_large(n_cells: int = 65536, intervals: int = 120, seed: int = 2) -> Workload:
     """Plain ROS3, 210 species / 500 reactions, 65,536 cells in groups of 32,
     T U[200, 310] K, p U[10, 1000] hPa setting [M], dt = 30 s x 120 intervals,

@@ -231,6 +231,36 @@ int fo_update_photolysis_clock(int32_t C, int32_t nphoto, const int32_t* rxn, co
                                int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
 int fo_advance_clock(double* t_dev, double dt, void* stream);
 
+/*
+ * Discrete adjoint of one interval (no counterpart in the reference, which has
+ * no sensitivities). With the accepted step sizes of a forward run held fixed
+ * (steps[step_ptr[g] .. step_ptr[g+1]) for group g, in order), the interval
+ * maps its start state Y (the checkpoint, device) and the log rate constants
+ * to its clamped end state through the steps of fastode/solvers.py:54-97.
+ *
+ * mode 0 (replay): writes that end state into Yout — the fixed-step map that
+ *        finite differences are taken of.
+ * mode 1 (adjoint): lam holds dL/dY at the interval end on entry and dL/dY at
+ *        the interval start on return; thbar (C x R via its strides) gains
+ *        dL/dlog k of every cell and reaction.
+ * Groups with more than max_steps steps get FO_STATUS_TOO_MANY_STEPS; a
+ * non-finite adjoint FO_STATUS_NAN_OR_INF. Workspace: fo_adjoint_workspace_bytes.
+ * One block per group; the projection of constrained systems is not
+ * differentiated (their checkpoints are taken after it).
+ */
+int fo_adjoint_workspace_bytes(const fo_plan* plan, int32_t ngroups, int32_t max_group_cells, int32_t max_steps,
+                               size_t* bytes);
+int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
+                        int32_t max_group_cells,
+                        const double* Y, int64_t y_cell_stride, int64_t y_species_stride,
+                        const double* k, int64_t k_cell_stride, int64_t k_reaction_stride,
+                        const double* atol, double dt,
+                        const int32_t* step_ptr, const double* steps, int32_t max_steps, int32_t mode,
+                        double* lam, int64_t lam_cell_stride, int64_t lam_species_stride,
+                        double* thbar, int64_t thbar_cell_stride, int64_t thbar_reaction_stride,
+                        double* Yout, int64_t yout_cell_stride, int64_t yout_species_stride,
+                        int32_t* status, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Forcing F(Y) (C x n, written with the Y strides into F) for C cells:
  * fastode.chem.Mechanism.rhs (fastode/chem.py:89-90). Device pointers. */
 int fo_eval_rhs(const fo_plan* plan, int32_t C,

@@ -132,7 +132,8 @@ class OChem:
         cnt = np.bincount(self.cols, minlength=self.n)
         self.block_indices = self.rows[self.order]
         self.block_indptr = np.concatenate([[0], np.cumsum(cnt)])
-        self.k = np.atleast_2d(np.asarray(k, dtype=np.float64))
+        k = np.atleast_2d(np.asarray(k))
+        self.k = k if np.iscomplexobj(k) else k.astype(np.float64)     # complex: complex-step tangents
         self.mass = np.ones(self.n) if mass is None else np.asarray(mass, dtype=float)
         self.dense = (self.n <= 60) if dense is None else dense
 
@@ -167,7 +168,7 @@ class OChem:
         vals = self.jac_values(Y)
         if not self.dense:
             return vals
-        J = np.zeros((vals.shape[0], self.n, self.n))
+        J = np.zeros((vals.shape[0], self.n, self.n), dtype=vals.dtype)
         J[:, self.rows, self.cols] = vals
         return J
 
@@ -517,3 +518,35 @@ def run_groups(mech, Y0, k_at, dt, intervals, atol, rtol, group_size=32, tableau
         memories.append(mem)
         traces.append(alg.trace)
     return Y, counts, statuses, memories, traces
+
+
+# ---- the fixed-step map and its tangent (checks the device adjoint) ----------------
+
+def replay_interval(system, tab, Y, steps):
+    """The given step sizes in order with no error control (the accepted
+    steps of a forward call, held fixed; fastode/solvers.py:494-504 with
+    per-step sizes), then the clamp of fastode/solvers.py:89-97 written with a
+    mask so that complex (complex-step) states pass through it."""
+    for h in steps:
+        F0 = system.rhs(Y)
+        J = system.jac(Y)
+        LU = system.factor(1.0 / (h * tab.gamma), J)
+        Y, _ = stages(system, tab, Y, F0, LU, h, OCounts())
+    keep = np.real(Y) > 0.0
+    if system.has_constraints:
+        keep = keep | (system.mass != 1.0)[None, :]
+    return np.where(keep, Y, 0.0)
+
+
+def tangent_linear(mech, Y0, dY0, k_list, dlogk, steps_list, tab=None, mass=None, eps=1e-30):
+    """Directional derivative of the fixed-step map over all intervals in
+    direction (dY0, dlogk) by the complex step: exact to roundoff, because the
+    map is analytic in its inputs away from the clamp's kink. k_list[i] is
+    (C, R); steps_list[i] is the list of step sizes of interval i."""
+    tab = tab or OROS3
+    Y = Y0.astype(np.complex128) + 1j * eps * dY0
+    scale = np.exp(1j * eps * np.asarray(dlogk))[None, :]
+    for k, steps in zip(k_list, steps_list):
+        system = OChem(mech, k.astype(np.complex128) * scale, mass=mass, dense=True)
+        Y = replay_interval(system, tab, Y, steps)
+    return np.imag(Y) / eps, np.real(Y)

@@ -168,6 +168,28 @@ def main():
     import fastode
     from fastode_gb300 import synthetic as syn
 
+    # the constrained synthetic workload: one group of 32 cells, RODAS3 with the
+    # projection at every call
+    wl = syn.dae_constrained(n_cells=32, intervals=4)
+    from fastode import Algorithm, Counts, RODAS3
+    from fastode.chem import ChemSystem, Mechanism
+    rm = Mechanism(wl.sm.species, wl.sm.reactions)
+    alg = Algorithm(RODAS3)
+    mem = alg.new_memory()
+    c = Counts()
+    Y = wl.cells.Y0.copy()
+    ks = np.stack([wl.k_at(i) for i in range(wl.intervals)])
+    status = []
+    for i in range(wl.intervals):
+        Y, st = alg.solve(ChemSystem(rm, ks[i], mass=wl.mass), Y, wl.dt, wl.atol, wl.rtol, c, mem)
+        status.append(STATUS[st])
+    rt, pt, yt = reaction_tables(wl.sm)
+    np.savez_compressed(HERE / "rodas3_dae_160x340.npz", n=wl.sm.n, reactants=rt, products=pt, yields=yt,
+                        mass=wl.mass, Y0=wl.cells.Y0, k=ks, dt=wl.dt, intervals=wl.intervals, rtol=wl.rtol,
+                        atol=wl.atol, Y=Y, counts=np.array(list(c.as_dict().values())), status=np.array(status),
+                        memory=np.array([mem.h_next, mem.err_prev, mem.h_prev]))
+    print("rodas3_dae_160x340 counts", list(c.as_dict().values()), "status", status)
+
     for name, arrays in dae_cases().items():
         np.savez_compressed(HERE / f"{name}.npz", **arrays)
         print(name, "counts", arrays["counts"].tolist(), "status", arrays["status"].tolist())

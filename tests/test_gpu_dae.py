@@ -49,3 +49,26 @@ def test_rodas3_projection_matches_reference(cuda, case, kernel):
     assert extra[4] == extra[5] == extra[6]
     assert mem.h_next == f["memory"][0]
     assert rel_err(Y, f["Y"], floor=1e-300 + np.abs(f["atol"]).max() * 1e-4).max() <= 1e-9
+
+
+@pytest.mark.parametrize("kernel", ["pipelined", "plain"])
+def test_constrained_synthetic_matches_reference(cuda, kernel):
+    """The constrained synthetic workload (150 differential + 10 quasi-steady
+    species, one group of 32 cells, four 60 s intervals, RODAS3 at rtol 1e-4):
+    the reference's Counts (projection passes and line-search trials included)
+    and statuses; states within 1e-9 relative."""
+    from golden_cases import mechanism_of
+    from fastode_gb300.batch import Batch
+    from fastode_gb300 import RODAS3, Algorithm
+    torch = cuda
+    f = load("rodas3_dae_160x340")
+    mech = mechanism_of(f)
+    b = Batch(mech, f["Y0"], group_size=32, algorithm=Algorithm(RODAS3, kernel=kernel), mass=f["mass"])
+    atol = torch.from_numpy(f["atol"]).cuda()
+    st = []
+    for i in range(int(f["intervals"])):
+        b.step(torch.from_numpy(np.ascontiguousarray(f["k"][i].T)).cuda(), float(f["dt"]), atol, float(f["rtol"]))
+        st.append(int(b.status.cpu().numpy()[0]))
+    assert st == list(f["status"])
+    np.testing.assert_array_equal(b.counts.cpu().numpy()[0], f["counts"])
+    assert rel_err(b.state(), f["Y"]).max() <= 1e-9

@@ -70,7 +70,7 @@ def test_multi_matches_oracle_on_dark_and_lit_cells(cuda):
     wls = small_parts()
     mb = MultiBatch_from(wls, cuda)
     mb.run(2, graph=True)
-    cuda.synchronize()
+    cuda.cuda.synchronize()
     for wl, part in zip(wls, mb.parts):
         assert np.any(wl.k_at(0)[:, wl.sm.photolytic] == 0.0)      # some cells dark
         Yo, co, _, _, _ = O.run_groups(wl.sm.mech, wl.cells.Y0, wl.k_at, wl.dt, 2, wl.atol, wl.rtol)

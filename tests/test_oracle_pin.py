@@ -170,3 +170,26 @@ def test_oracle_reproduces_reference_dae_fixture(case):
     assert status == list(f["status"])
     assert (mem.h_next, mem.err_prev, mem.h_prev) == tuple(f["memory"])
     np.testing.assert_array_equal(Y, f["Y"])
+
+
+def test_oracle_tangent_linear_matches_central_differences():
+    """The host FP64 tangent-linear of the fixed-step map (complex step
+    through the oracle's own steps) agrees with central differences, h = 1e-6."""
+    f = load("ros3_20x40")
+    mech = mechanism_of(f)
+    Y0 = f["Y0"][:32]
+    ks = [f["k"][i][:32] for i in range(3)]
+    steps = [[30.0], [15.0, 15.0], [30.0]]
+    rng = np.random.default_rng(0)
+    dY = Y0 * rng.standard_normal(Y0.shape)
+    dth = rng.standard_normal(mech.R)
+    tl, _ = O.tangent_linear(mech, Y0, dY, ks, dth, steps)
+
+    def run(Y, th):
+        for k, s in zip(ks, steps):
+            Y = O.replay_interval(O.OChem(mech, k * np.exp(th)[None, :], dense=True), O.OROS3, Y, s)
+        return Y
+
+    h = 1e-6
+    fd = (run(Y0 + h * dY, h * dth) - run(Y0 - h * dY, -h * dth)) / (2 * h)
+    assert np.max(np.abs(tl - fd)) <= 1e-8 * np.max(np.abs(tl))
