@@ -298,6 +298,131 @@ def run_ours(args, rank, world):
     return out
 
 
+def _device_rates(lib, sm, cells, dev, sp):
+    """(R, C) thermal rate constants computed on the device, plus what the
+    photolysis update needs."""
+    import ctypes as C
+    import torch
+    from fastode_gb300 import _abi, synthetic as syn
+    Cc, R = cells.C, sm.R
+    M = cells.p / (syn.R_GAS * cells.T)
+    photo = np.nonzero(sm.photolytic)[0].astype(np.int32)
+    d = {name: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for name, v in
+         dict(A=sm.A, E=sm.E, power=sm.mech.third_body_power, T=cells.T, M=M).items()}
+    k = torch.empty((R, Cc), dtype=torch.float64, device=dev)
+    _abi.check(lib.fo_rate_constants(Cc, R, d["A"].data_ptr(), d["E"].data_ptr(), d["power"].data_ptr(),
+                                     d["T"].data_ptr(), d["M"].data_ptr(), k.data_ptr(), 1, Cc, sp),
+               "fo_rate_constants")
+    return k, photo
+
+
+def run_batched(args):
+    """Batched uneven workload: 1,048,576 cells over three synthetic mechanisms
+    (60/40, 120/260, 210/500) in one persistent launch per interval, photolysis
+    under a diurnal cosine (half the cells dark), dt = 60 s, each interval one
+    replay of a captured CUDA graph."""
+    import ctypes as C
+    import torch
+    from fastode_gb300 import _abi, build as fbuild, synthetic as syn
+    from fastode_gb300.multi import MultiBatch, Part
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    lib = _abi.lib()
+    sp = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    wls = syn.batched_uneven(n_cells=args.cells, intervals=args.steps)
+    parts = []
+    for wl in wls:
+        k, photo = _device_rates(lib, wl.sm, wl.cells, dev, sp)
+        p = Part(wl.sm.mech, torch.from_numpy(wl.cells.Y0).to(dev), k.t(), wl.atol, wl.rtol, wl.dt,
+                 photolysis=(photo, wl.sm.J[photo], wl.cells.phase))
+        parts.append(p)
+    mb = MultiBatch(parts)
+    mb.capture()
+    mb.run(args.warmup, graph=True)
+    torch.cuda.synchronize()
+    mb.reset()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clocks:
+        e0.record()
+        mb.run(args.steps, graph=True)
+        e1.record()
+        torch.cuda.synchronize()
+    s = e0.elapsed_time(e1) / 1e3
+    total = sum(p.C for p in parts)
+    per_part = []
+    for wl, p in zip(wls, parts):
+        c = p.counts.cpu().numpy()
+        st = p.status.cpu().numpy()
+        per_part.append({"mechanism": wl.name, "cells": p.C, "attempts_per_group_interval":
+                         float(c[:, 0].sum() / len(c) / args.steps), "non_converged_groups": int((st != 0).sum()),
+                         "plan": {k: v for k, v in p.plan.info.items() if k in ("nnz_lu", "lu_fma", "ordering")}})
+    return {"metric": METRIC, "value": total * args.steps / s, "unit": "cell-intervals/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": s / args.steps * 1e3,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": "batched uneven: %d cells over 60/40, 120/260, 210/500, dt=60 s, half dark, "
+                                   "one persistent launch per interval replayed as a CUDA graph" % total,
+                       "slots": mb.slots},
+            "gpu_launches": args.steps * mb.launches_per_interval(), "parts": per_part, "clocks": clocks.summary()}
+
+
+def run_adjoint(args):
+    """Adjoint cost: (forward + adjoint) / forward for the 210/500 mechanism,
+    4,096 cells, 60 intervals of 30 s; loss = sum_i (log(y_i + a) - log(yhat_i + a))^2
+    over final states with targets from a perturbed-rate forward run
+    (log k + N(0, 0.1)); two central-difference directions (h = 1e-6) of the
+    fixed-step replay check the gradient."""
+    import torch
+    from fastode_gb300 import adjoint as A, build as fbuild, synthetic as syn
+    from fastode_gb300.batch import Batch
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    wl = syn.plain_large(n_cells=args.cells, intervals=args.steps)
+    ks = [torch.from_numpy(np.ascontiguousarray(wl.k_at(i).T)).to(dev) for i in range(args.steps)]
+    rng = np.random.default_rng(11)
+    pert = torch.from_numpy(np.exp(rng.normal(0.0, 0.1, wl.sm.R))).to(dev)[:, None]
+    a = 1e-14
+    atol = torch.from_numpy(wl.atol).to(dev)
+
+    def forward(kk):
+        b = Batch(wl.sm.mech, wl.cells.Y0, group_size=32)
+        for i in range(args.steps):
+            b.step(kk[i], wl.dt, atol, wl.rtol)
+        return b
+
+    target = forward([k * pert for k in ks]).Y.clone()
+    forward(ks)                                                    # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fb = forward(ks)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    traj = A.forward_record(wl.sm.mech, wl.cells.Y0, lambda i: ks[i], wl.dt, wl.atol, wl.rtol, args.steps)
+    Y = traj.batch.Y
+    lam = 2.0 * (torch.log(Y + a) - torch.log(target + a)) / (Y + a)
+    lam0, thbar = A.adjoint(traj, lam)
+    torch.cuda.synchronize()
+    t_fa = time.perf_counter() - t0
+    g_th = thbar.sum(dim=1).cpu().numpy()
+
+    def loss(Yend):
+        return float(((torch.log(Yend + a) - torch.log(target + a)) ** 2).sum())
+
+    checks = []
+    h = 1e-6
+    for d in range(2):
+        dth = rng.standard_normal(wl.sm.R)
+        sc = [torch.from_numpy(np.exp(s * h * dth)).to(dev)[:, None] for s in (1.0, -1.0)]
+        fd = (loss(A.replay(traj, ks=[k * sc[0] for k in ks])) - loss(A.replay(traj, ks=[k * sc[1] for k in ks]))) / (2 * h)
+        adj = float(np.dot(g_th, dth))
+        checks.append({"fd": fd, "adjoint": adj, "rel": abs(fd - adj) / max(abs(fd), 1e-300)})
+    return {"metric": "adjoint/forward cost", "value": t_fa / t_fwd, "unit": "ratio", "higher_is_better": False,
+            "forward_s": t_fwd, "forward_plus_adjoint_s": t_fa, "max_steps_per_interval": traj.max_steps,
+            "config": {"workload": f"adjoint ROS3 210x500, {args.cells} cells, {args.steps} x 30 s, "
+                                   "gradients w.r.t. 500 log rate constants and the initial state"},
+            "fd_checks": checks}
+
+
 def run_reference(args, rank, world):
     """The reference's CPU path (the oracle port: the reference is Python and
     does not travel) on every host core: each step advances one group per
@@ -342,11 +467,17 @@ def main():
     ap.add_argument("--cpu-intervals", type=int, default=30)
     ap.add_argument("--cpu-workers", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"],
+                    help="plain: the 210/500 drop-in workload (default, the headline line); batched: the "
+                         "three-mechanism persistent launch; adjoint: forward+adjoint cost")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload != "plain" and args.impl == "ours":
+        print(json.dumps(run_batched(args) if args.workload == "batched" else run_adjoint(args)))
+        return
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args, rank, world)))

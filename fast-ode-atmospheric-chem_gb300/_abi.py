@@ -46,7 +46,8 @@ class Options(C.Structure):
     _fields_ = [("tableau", C.c_int32), ("controller", C.c_int32), ("b", C.c_double),
                 ("safety", C.c_double), ("fac_min", C.c_double), ("fac_max", C.c_double),
                 ("carry", C.c_int32), ("quantize", C.c_int32), ("carry_memory", C.c_int32),
-                ("max_steps", C.c_int32), ("variant", C.c_int32)]
+                ("max_steps", C.c_int32), ("variant", C.c_int32), ("loop", C.c_int32),
+                ("step_change_rows", C.c_int32)]
 
 
 VARIANTS = {"pipelined": 0, "plain": 1}

@@ -304,6 +304,9 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
   p.o.carry_memory = opt->carry_memory;
   p.o.max_steps = opt->max_steps;
   p.o.variant = opt->variant;
+  if (opt->loop != FO_LOOP_ALGORITHM && opt->loop != FO_LOOP_RESTARTING) return fail(FO_E_INVALID, "unknown loop");
+  p.o.loop = opt->loop;
+  p.o.step_change_rows = opt->step_change_rows;
   // the pipelined kernel needs the packed stream (positions below 65,536 and
   // rows shorter than 32,767 entries); larger mechanisms run the plain loops
   if (p.o.variant == FO_VARIANT_PIPELINED && plan->dev.elp == nullptr) p.o.variant = FO_VARIANT_PLAIN;

@@ -53,6 +53,8 @@ struct DevOptions {
   double b, safety, fac_min, fac_max;
   int carry, quantize, carry_memory, max_steps;
   int variant;     // FO_VARIANT_*
+  int loop;        // FO_LOOP_*
+  int step_change_rows;
   double k_exp;    // embedded order + 1
 };
 

@@ -287,8 +287,6 @@ __device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln,
     }
     if (kRingChunks - 1 < nch) meta_load(meta + (kRingChunks - 1) * kChunk, mi);
     if (nch > 0) meta_load(meta, mc);
-    Meta mp;                  // the previous chunk, computed but not yet written back
-    double wp[kChunk];
 #pragma unroll 1
     for (int c = 0; c < nch; ++c) {
       const int ahead = c + kRingChunks - 1;
@@ -301,14 +299,10 @@ __device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln,
       double wc[kChunk];
       chunk_read(mc, w, L, lane, wc);
       chunk_fma(mc, ring + (int64_t)(c % kRingChunks) * kChunk * L, lu, L, lane, wc, l, q);
-      if (c > 0) chunk_write(mp, w, L, lane, wp);
-      mp = mc;
-#pragma unroll
-      for (int s = 0; s < kChunk; ++s) wp[s] = wc[s];
+      chunk_write(mc, w, L, lane, wc);
       mi = mi_next;
       mc = mc_next;
     }
-    if (nch > 0) chunk_write(mp, w, L, lane, wp);
     SCR(lu, dg) = 1.0 / WROW(dg - q0);
     for (int qq = dg + 1; qq < q1; ++qq) SCR(lu, qq) = WROW(qq - q0);
   }
@@ -490,6 +484,10 @@ __device__ __noinline__ double attempt(const SolveParams& p, const Lane& ln, dou
       if (tb.e[r] != 0.0) e = __dadd_rn(e, __dmul_rn(tb.e[r], kv));
     }
     SCR(Ynew, i) = yn;
+    // the restarting loop replaces the algebraic rows of the estimate by the
+    // step change (fastode/solvers.py:238-239)
+    if (p.o.loop == FO_LOOP_RESTARTING && p.o.step_change_rows && dae && __ldg(p.t.mass + i) == 0.0)
+      e = __dsub_rn(yn, y);
     const double ymax = npmax(fabs(y), fabs(yn));
     const double s = __ddiv_rn(e, __dadd_rn(__ldg(p.atol + __ldg(p.t.perm + i)), __dmul_rn(p.rtol, ymax)));
     acc = __dadd_rn(acc, __dmul_rn(s, s));
@@ -665,7 +663,132 @@ __device__ __noinline__ bool project(const SolveParams& p, const Lane& ln, doubl
 }
 
 // One group over one interval: fastode/solvers.py:305-415 statement by statement.
+// The baseline restarting loop, fastode/solvers.py:205-267 statement by
+// statement: a restart at 1e-6 of the interval, the elementary controller,
+// no carried memory, "too many steps" past max_steps attempts.
+__device__ __noinline__ void solve_group_restarting(const SolveParams& p, int g, double* scr, double* w,
+                                                    double* red) {
+  const int L = blockDim.x, lane = threadIdx.x;
+  const int n = p.t.n;
+  const int64_t c0 = p.group_offsets[g], C = p.group_offsets[g + 1] - c0;
+  Lane ln;
+  ln.lane = lane;
+  ln.L = L;
+  ln.active = lane < C;
+  ln.cell = c0 + (ln.active ? lane : (C - 1));
+  const DevOptions& o = p.o;
+  const double dt = p.dt;
+  long long c_steps = 0, c_acc = 0, c_rej = 0, c_rhs = 0, c_jac = 0, c_lu = 0, c_solves = 0;
+  int nrec = 0;
+  double* Y = scr + p.sl.y * L;
+  double* Ynew = scr + p.sl.ynew * L;
+  double* F0 = scr + p.sl.f0 * L;
+  double* negj = scr + p.sl.negj * L;
+  double* dd = scr + p.sl.d * L;
+  double* rr = scr + p.sl.r * L;
+  double* lu = scr + p.sl.lu * L;
+  for (int i = 0; i < n; ++i) SCR(Y, i) = p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss];
+  const double rounding = 2.220446049250313e-16;
+  const double h_min = __dmul_rn(1.0e-15, dt);
+  const double h_max = dt;
+  double H = pymin(pymax(h_min, __dmul_rn(1.0e-6, dt)), h_max);
+  const double elem_exp = 1.0 / o.k_exp;
+  const double nsize = (double)(C * n);
+  int status = -1;
+  ProjectionCounts pc;
+  if (p.t.has_constraints && !project(p, ln, Y, scr, w, red, pc)) status = FO_STATUS_PROJECTION_FAILED;
+  c_rhs += pc.rhs;
+  c_jac += pc.jac;
+  c_lu += pc.lu;
+  c_solves += pc.solves;
+  double t = 0.0;
+  bool reject_last = false, reject_more = false;
+  int nsteps = 0;
+  while (status < 0 && __dadd_rn(__dsub_rn(t, dt), rounding) <= 0.0) {
+    if (nsteps > o.max_steps) {
+      status = FO_STATUS_TOO_MANY_STEPS;
+      break;
+    }
+    if (__dadd_rn(t, __dmul_rn(0.1, H)) == t || H <= pymin(rounding, h_min)) {
+      status = FO_STATUS_STEP_TOO_SMALL;
+      break;
+    }
+    H = pymin(H, fabs(__dsub_rn(dt, t)));
+    eval_rhs(p, ln, Y, rr, F0);
+    ++c_rhs;
+    eval_negjac(p, ln, Y, dd, negj);
+    ++c_jac;
+    bool accepted = false;
+    while (!accepted) {
+      factor_any(p, ln, 1.0 / __dmul_rn(H, o.tab.gamma), negj, lu, w, false);
+      ++c_lu;
+      const double total = block_sum(attempt(p, ln, H, Y, Ynew, scr, w, c_rhs, c_solves), red);
+      double err = sqrt(__ddiv_rn(total, nsize));
+      if (!isnan(err)) err = pymax(err, 1.0e-10);
+      ++nsteps;
+      ++c_steps;
+      if (isnan(err) || isinf(err)) {
+        trace_record(p, g, nrec, t, H, err, -1.0);
+        status = FO_STATUS_NAN_OR_INF;
+        break;
+      }
+      const double fac = pymin(6.0, pymax(0.2, __ddiv_rn(0.9, pow(err, elem_exp))));
+      double Hnew = __dmul_rn(H, fac);
+      if (err < 1.0 || H < h_min) {
+        trace_record(p, g, nrec, t, H, err, 1.0);
+        ++c_acc;
+        t = __dadd_rn(t, H);
+        double* tmp = Y;
+        Y = Ynew;
+        Ynew = tmp;
+        Hnew = pymax(h_min, pymin(Hnew, h_max));
+        if (reject_last) Hnew = pymin(Hnew, H);
+        reject_last = reject_more = false;
+        H = Hnew;
+        accepted = true;
+      } else {
+        trace_record(p, g, nrec, t, H, err, 0.0);
+        if (reject_more) Hnew = __dmul_rn(H, 0.1);
+        reject_more = reject_last;
+        reject_last = true;
+        H = Hnew;
+        ++c_rej;
+      }
+    }
+  }
+  if (status < 0) status = FO_STATUS_CONVERGED;
+  const bool clamp = status != FO_STATUS_PROJECTION_FAILED;
+  if (ln.active)
+    for (int i = 0; i < n; ++i) {
+      double y = SCR(Y, i);
+      if (clamp && (!p.t.has_constraints || __ldg(p.t.mass + i) == 1.0)) y = clamp0(y);
+      p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss] = y;
+    }
+  if (threadIdx.x == 0) {
+    long long* cn = p.counts + (int64_t)g * FO_NUM_COUNTS;
+    cn[0] += c_steps;
+    cn[1] += c_acc;
+    cn[2] += c_rej;
+    cn[3] += c_rhs;
+    cn[4] += c_jac;
+    cn[5] += c_lu;
+    cn[6] += c_solves;
+    cn[10] += pc.passes;
+    cn[11] += pc.trials;
+    cn[12] += 1;
+    p.status[g] = status;
+    if (p.trace_len) p.trace_len[g] = nrec;
+  }
+}
+
+__device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, double* w, double* red);
+
 __device__ void solve_group(const SolveParams& p, int g, double* scr, double* w, double* red) {
+  if (p.o.loop == FO_LOOP_RESTARTING) solve_group_restarting(p, g, scr, w, red);
+  else solve_group_algorithm(p, g, scr, w, red);
+}
+
+__device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, double* w, double* red) {
   const int L = blockDim.x, lane = threadIdx.x;
   const int n = p.t.n;
   const int64_t c0 = p.group_offsets[g], c1 = p.group_offsets[g + 1];

@@ -9,6 +9,8 @@ namespace fo {
 constexpr int kStreamChunk = 16;
 // Chunks of the factorization's shared-memory prefetch ring.
 constexpr int kRingChunks = 5;
+// Chunks over which the elimination stream is hazard-free (see symbolic.cpp).
+constexpr int kHazardWindow = 1;
 // The no-op entry's y of the solve streams.
 constexpr int32_t kNoop = -2147483647 - 1;
 

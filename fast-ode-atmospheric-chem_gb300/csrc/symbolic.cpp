@@ -298,13 +298,13 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
   t->el_ptr.assign(1, 0);
   t->el.clear();
   t->max_row_len = 0;
-  // Every chunk is hazard-free over a window of two chunks: no slot is updated
-  // twice in a chunk, and no entry (update or multiplier) touches a slot that
-  // an earlier entry of the same chunk or of the previous chunk updated. The
-  // device then reads a chunk's work-row values at once, runs its updates as
-  // independent FMAs (only the multipliers chain them), and writes them back
-  // only after the next chunk's values are read and its FMAs issued: FP64
-  // latency overlaps instead of serializing every read-modify-write.
+  // Every chunk is hazard-free over a window of kHazardWindow chunks: no slot
+  // is updated twice in a chunk, and no entry (update or multiplier) touches a
+  // slot that an earlier entry of the same chunk (or, with a window of two, of
+  // the previous chunk) updated. The device then reads a chunk's work-row
+  // values at once, runs its updates as independent FMAs (only the multipliers
+  // chain them) and writes them back: FP64 latency overlaps instead of
+  // serializing every read-modify-write.
   std::vector<int> slot_of(n, -1);
   std::vector<int64_t> touched(n, -1);  // absolute chunk that last updated a slot
   auto entries = [&]() { return (int64_t)(t->el.size() / 2); };
@@ -330,12 +330,12 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
     for (int q = q0; q < t->lu_diag[r]; ++q) {
       const int k = t->lu_col[q];
       const int ym = q - q0;                        // the multiplier reads slot ym
-      while (touched[ym] >= entries() / kStreamChunk - 1) pad_chunk();
+      while (touched[ym] >= entries() / kStreamChunk - (kHazardWindow - 1)) pad_chunk();
       t->el.push_back(-1 - t->lu_diag[k]);
       t->el.push_back(ym);
       for (int u = t->lu_diag[k] + 1; u < t->lu_row_ptr[k + 1]; ++u) {
         const int y = slot_of[t->lu_col[u]];
-        while (touched[y] >= entries() / kStreamChunk - 1) pad_chunk();
+        while (touched[y] >= entries() / kStreamChunk - (kHazardWindow - 1)) pad_chunk();
         touched[y] = entries() / kStreamChunk;
         t->el.push_back(u);
         t->el.push_back(y);

@@ -121,7 +121,7 @@ class Algorithm:
         return _abi.Options(tableau_id(self.tableau), 0 if self.controller == "h211b" else 1,
                             float(self.b), float(self.safety), float(self.fac_min), float(self.fac_max),
                             int(bool(self.carry)), int(bool(self.quantize)), int(bool(self.carry_memory)),
-                            int(self.max_steps), _abi.VARIANTS[self.kernel])
+                            int(self.max_steps), _abi.VARIANTS[self.kernel], 0, 0)
 
     def solve(self, system, Y, dt, atol, rtol, counts: Counts, memory: Memory = None):
         """Integrate one group (all rows of Y) over one interval; returns
@@ -161,6 +161,34 @@ class Algorithm:
         mem.h_next, mem.err_prev, mem.h_prev = float(h[0]), float(h[1]), float(h[2])
         counts.add_row(cnt.cpu().numpy()[0])
         return Yd.cpu().numpy(), _abi.STATUS_STRINGS[int(st.cpu().item())]
+
+
+class RestartingLoop(Algorithm):
+    """The baseline Rosenbrock loop of fastode/solvers.py:189-267 on the GPU:
+    restarted at 1e-6 of the interval every call under the elementary
+    controller, no memory carried (``new_memory`` returns None, as in the
+    reference). step_change_rows: with constraints, the step change replaces
+    the algebraic rows of the error estimate."""
+
+    name = "restarting"
+
+    def __init__(self, tableau: Tableau = ROS3, max_steps: int = 1000, step_change_rows: bool = True,
+                 ordering: str = "auto", kernel: str = "pipelined"):
+        super().__init__(tableau, controller="elementary", max_steps=max_steps, ordering=ordering, kernel=kernel)
+        self.step_change_rows = step_change_rows
+
+    def new_memory(self):
+        return None
+
+    def options(self) -> _abi.Options:
+        o = super().options()
+        o.loop = 1
+        o.step_change_rows = int(bool(self.step_change_rows))
+        return o
+
+    def solve(self, system, Y, dt, atol, rtol, counts: Counts, memory=None):
+        """Integrate one group over one interval; returns (Y_new, status)."""
+        return super().solve(system, Y, dt, atol, rtol, counts, None)
 
 
 def _eval(system, Y, jac: bool):

@@ -116,7 +116,18 @@ typedef struct fo_options {
   int32_t carry_memory;       /* keep the filter memory across intervals */
   int32_t max_steps;          /* attempt budget per call (1000) */
   int32_t variant;            /* FO_VARIANT_*: which LU/solve kernel (same results up to roundoff) */
+  int32_t loop;               /* FO_LOOP_*: the step loop */
+  int32_t step_change_rows;   /* restarting loop with constraints: the step change replaces the
+                                 algebraic rows of the error estimate (fastode/solvers.py:194-200) */
 } fo_options;
+
+/* Step loops. ALGORITHM is fastode.solvers.Algorithm (fastode/solvers.py:270-415);
+ * RESTARTING is the baseline fastode.solvers.RestartingLoop (fastode/solvers.py:189-267):
+ * a restart at 1e-6 of the interval every call, the elementary controller, no
+ * carried memory (b, fac_min, fac_max, carry, quantize, carry_memory and the
+ * memory array are ignored; the memory array is neither read nor written). */
+#define FO_LOOP_ALGORITHM 0
+#define FO_LOOP_RESTARTING 1
 
 /* Kernel variants of the factorization and solves. PIPELINED streams the
  * elimination schedule with register double-buffering (the fast path);

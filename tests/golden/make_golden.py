@@ -159,6 +159,67 @@ def dae_cases():
     return out
 
 
+def ts1_case(reference):
+    """TS1 (209 species, 547 reactions, P = 3) on the tier1-30s scenario, 64
+    cells x 101 intervals, Algorithm(ROS3) at rtol 1e-3, atol 1e-17, through
+    the reference's own run_scenario (fastode/ts1.py:181-223). Stores what the
+    device needs to rebuild every interval's rate constants exactly as
+    run_scenario does (the static k, the photolysis columns' base values,
+    scaling factors and the scenario factor of every interval) and checks the
+    Counts against the archived record reference-results/ts1/runs.csv."""
+    import csv
+    from fastode import Algorithm, ROS3
+    from fastode.ts1 import TS1, Cells, Scenario, run_scenario
+
+    ts1 = TS1()
+    sc = Scenario(Path(reference) / "data/scenarios/tier1-30s/scenario.txt")
+    cells = Cells(ts1, sc.cells)
+    snaps, counts, statuses = run_scenario(sc, Algorithm(ROS3), cells, ts1, 1e-3, 1e-17)
+    with open(Path(reference) / "reference-results/ts1/runs.csv") as fh:
+        row = next(r for r in csv.DictReader(fh)
+                   if r["config"] == "alg" and r["scenario"] == "tier1-30s" and float(r["rtol"]) == 1e-3)
+    for field in ("steps", "accepted", "rejected", "rhs", "jac", "lu", "solves"):
+        assert int(row[field]) == getattr(counts, field), (field, row[field], getattr(counts, field))
+    photo = ts1.photolysis_reactions
+    names = [ts1.reactions[j]["MUSICA name"] for j in photo]
+    scaling = np.array([ts1.reactions[j].get("scaling factor", 1.0) for j in photo])
+    base = np.stack([cells.params[nm] for nm in names], axis=1)            # (C, nphoto)
+    f = np.array([sc.factor(i * sc.dt) for i in range(sc.steps)])
+    params0 = {k: (v * f[0] if k.startswith("j") else v) for k, v in cells.params.items()}
+    k_static = ts1.rate_constants(cells.T, cells.P, params0)
+    m = ts1.mech
+    Sr, Sc = np.nonzero(m.S)
+    GT = m.GT.tocsr()
+    # the controller variants and the restarting loop on the same scenario,
+    # each checked against its archived row (experiments/ts1_experiments.py:49-70)
+    from fastode import RestartingLoop
+    variants = {
+        "alg-elementary": (Algorithm(ROS3, controller="elementary"), 5e-4, 5e-18),
+        "alg-noquant": (Algorithm(ROS3, quantize=False), 5e-4, 5e-18),
+        "alg-nomemory": (Algorithm(ROS3, carry_memory=False), 5e-4, 5e-18),
+        "alg-reset": (Algorithm(ROS3, carry=False, quantize=False), 1e-2, 1e-16),
+        "restart": (RestartingLoop(ROS3), 1e-3, 1e-15),
+    }
+    extra = {}
+    for name, (solver, rtol, atol) in variants.items():
+        s_snaps, s_counts, _ = run_scenario(sc, solver, cells, ts1, rtol, atol)
+        with open(Path(reference) / "reference-results/ts1/runs.csv") as fh:
+            row = next(r for r in csv.DictReader(fh)
+                       if r["config"] == name and r["scenario"] == "tier1-30s" and float(r["rtol"]) == rtol)
+        for field in ("steps", "accepted", "rejected", "rhs", "jac", "lu", "solves"):
+            assert int(row[field]) == getattr(s_counts, field), (name, field)
+        key = name.replace("-", "_")
+        extra[f"{key}_Y"] = s_snaps[sc.steps]
+        extra[f"{key}_counts"] = np.array(list(s_counts.as_dict().values()))
+        extra[f"{key}_tol"] = np.array([rtol, atol])
+    return dict(m_n=m.n, m_R=m.R, m_P=m.P, m_react=m.react, m_S_rows=Sr, m_S_cols=Sc, m_S_vals=m.S[Sr, Sc], **extra,
+                m_rows=m.pattern.rows, m_cols=m.pattern.cols, m_gt_indptr=GT.indptr, m_gt_indices=GT.indices,
+                m_gt_data=GT.data, Y0=cells.Y, k_static=k_static, photo=np.array(photo), base=base,
+                scaling=scaling, f=f, dt=sc.dt, intervals=sc.steps, rtol=1e-3, atol=np.full(m.n, 1e-17),
+                group_size=32, Y=snaps[sc.steps], counts=np.array(list(counts.as_dict().values())),
+                n_failed=len(statuses))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -167,6 +228,10 @@ def main():
     sys.path.insert(0, str(ROOT))
     import fastode
     from fastode_gb300 import synthetic as syn
+
+    ts1 = ts1_case(a.reference)
+    np.savez_compressed(HERE / "ts1_tier1_30s.npz", **ts1)
+    print("ts1_tier1_30s counts", ts1["counts"].tolist())
 
     # the constrained synthetic workload: one group of 32 cells, RODAS3 with the
     # projection at every call

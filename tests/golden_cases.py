@@ -67,3 +67,21 @@ class TableMechanism:
         J = np.zeros((vals.shape[0], self.n, self.n))
         J[:, self.pattern.rows, self.pattern.cols] = vals
         return J
+
+
+def table_mechanism(f):
+    """TableMechanism from a fixture that stores S as COO (m_S_rows/cols/vals)."""
+    if "m_S" not in f:
+        S = np.zeros((int(f["m_n"]), int(f["m_R"])))
+        S[f["m_S_rows"], f["m_S_cols"]] = f["m_S_vals"]
+        f = dict(f, m_S=S)
+    return TableMechanism(f)
+
+
+def ts1_k(f, i):
+    """Rate constants of interval i of the TS1 fixture, built as the
+    reference's run_scenario builds them (fastode/ts1.py:204-214): the static
+    k with every photolysis column set to (base * f(t)) * scaling."""
+    k = np.array(f["k_static"], copy=True)
+    k[:, f["photo"]] = (f["base"] * f["f"][i]) * f["scaling"][None, :]
+    return k

@@ -1,0 +1,63 @@
+"""TS1 (209 species, 547 reactions with three-reactant rows) through the device
+integrator on the reference's tier1-30s scenario: 64 cells in groups of 32,
+101 intervals of 30 s, Algorithm(ROS3) at rtol 1e-3, atol 1e-17. The fixture
+was made by running the reference's run_scenario (tests/golden/make_golden.py)
+and its Counts equal the archived record reference-results/ts1/runs.csv
+(alg, rtol 1e-3, tier1-30s: 334 steps, 330 accepted, 4 rejected)."""
+import numpy as np
+import pytest
+
+from golden_cases import load, rel_err, table_mechanism, ts1_k
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("kernel", ["pipelined", "plain"])
+def test_ts1_tier1_counts_match_the_archive(cuda, kernel):
+    from fastode_gb300 import Algorithm
+    from fastode_gb300.batch import Batch
+    torch = cuda
+    f = load("ts1_tier1_30s")
+    mech = table_mechanism(f)
+    b = Batch(mech, f["Y0"], group_size=int(f["group_size"]), algorithm=Algorithm(kernel=kernel))
+    atol = torch.from_numpy(f["atol"]).cuda()
+    for i in range(int(f["intervals"])):
+        b.step(torch.from_numpy(np.ascontiguousarray(ts1_k(f, i).T)).cuda(), float(f["dt"]), atol, float(f["rtol"]))
+        assert all(s == "converged" for s in b.statuses())
+    total = b.counts.cpu().numpy().sum(axis=0)
+    np.testing.assert_array_equal(total, f["counts"])
+    assert total[0] == 334 and total[1] == 330 and total[2] == 4
+    err = rel_err(b.state(), f["Y"])
+    assert err.max() <= 1e-8, err.max()
+
+
+VARIANTS = {
+    # name: (solver factory, fixture key)
+    "alg-elementary": (lambda A, R, T: A(T, controller="elementary"), "alg_elementary"),
+    "alg-noquant": (lambda A, R, T: A(T, quantize=False), "alg_noquant"),
+    "alg-nomemory": (lambda A, R, T: A(T, carry_memory=False), "alg_nomemory"),
+    "alg-reset": (lambda A, R, T: A(T, carry=False, quantize=False), "alg_reset"),
+    "restart": (lambda A, R, T: R(T), "restart"),
+}
+
+
+@pytest.mark.parametrize("variant", sorted(VARIANTS))
+def test_ts1_controller_variants_and_restarting_loop(cuda, variant):
+    """The controller options of Algorithm (elementary controller, no
+    quantization, no carried filter memory, no carried step) and the
+    restarting loop on TS1 tier1-30s: the reference's Counts, which equal the
+    archived rows of reference-results/ts1/runs.csv for these configurations
+    (experiments/ts1_experiments.py:49-70)."""
+    from fastode_gb300 import ROS3, Algorithm, RestartingLoop
+    from fastode_gb300.batch import Batch
+    torch = cuda
+    f = load("ts1_tier1_30s")
+    make, key = VARIANTS[variant]
+    rtol, atol_v = f[f"{key}_tol"]
+    mech = table_mechanism(f)
+    b = Batch(mech, f["Y0"], group_size=int(f["group_size"]), algorithm=make(Algorithm, RestartingLoop, ROS3))
+    atol = torch.full((mech.n,), float(atol_v), dtype=torch.float64, device="cuda")
+    for i in range(int(f["intervals"])):
+        b.step(torch.from_numpy(np.ascontiguousarray(ts1_k(f, i).T)).cuda(), float(f["dt"]), atol, float(rtol))
+    np.testing.assert_array_equal(b.counts.cpu().numpy().sum(axis=0), f[f"{key}_counts"])
+    assert rel_err(b.state(), f[f"{key}_Y"]).max() <= 1e-8

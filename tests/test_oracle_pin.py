@@ -193,3 +193,17 @@ def test_oracle_tangent_linear_matches_central_differences():
     h = 1e-6
     fd = (run(Y0 + h * dY, h * dth) - run(Y0 - h * dY, -h * dth)) / (2 * h)
     assert np.max(np.abs(tl - fd)) <= 1e-8 * np.max(np.abs(tl))
+
+
+def test_oracle_reproduces_ts1_tier1_archive():
+    """TS1 on tier1-30s through the oracle (SuperLU path, as the reference's
+    run_scenario uses): the archived Counts (334 / 330 / 4) and the reference's
+    final states bit for bit."""
+    from golden_cases import table_mechanism, ts1_k
+    f = load("ts1_tier1_30s")
+    mech = table_mechanism(f)
+    Y, counts, statuses, _, _ = O.run_groups(mech, f["Y0"], lambda i: ts1_k(f, i), float(f["dt"]),
+                                             int(f["intervals"]), f["atol"], float(f["rtol"]), group_size=32)
+    total = np.sum([c.as_tuple() for c in counts], axis=0)
+    np.testing.assert_array_equal(total, f["counts"])
+    np.testing.assert_array_equal(Y, f["Y"])
