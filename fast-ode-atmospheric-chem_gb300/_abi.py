@@ -79,6 +79,8 @@ SIGNATURES = {
     "fo_solve": (C.c_int, [_P, C.POINTER(Options), _I32, _P, _I32,
                            _P, _I64, _I64, _P, _I64, _I64, _P, _D, _D,
                            _P, _P, _P, _P, C.c_size_t, _I32, _P, _I32, _P, _P]),
+    "fo_solve_static": (C.c_int, [_P, C.POINTER(Options), _I32, _P, _I32,
+                                  _P, _I64, _I64, _P, _I64, _I64, _P, _D, _D, _P, _P, _P, _P]),
     "fo_eval_rhs": (C.c_int, [_P, _I32, _P, _I64, _I64, _P, _I64, _I64, _P, _P]),
     "fo_eval_jac": (C.c_int, [_P, _I32, _P, _I64, _I64, _P, _I64, _I64, _P, _P]),
     "fo_rate_constants": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),

@@ -18,6 +18,7 @@ namespace fo {
 cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream);
 cudaError_t launch_eval(const SolveParams& p, int C, int want_jac, double* out, cudaStream_t stream);
 cudaError_t launch_adjoint(const AdjParams& a, int grid, int lanes, size_t smem, cudaStream_t stream);
+int set_last_error(int code, const char* what);
 cudaError_t launch_solve_multi(const SolveParams* batches, int nb, const int32_t* starts, int32_t* queue,
                                double* scratch, int64_t slot_doubles, int grid, int lanes, size_t smem,
                                cudaStream_t stream);
@@ -43,6 +44,13 @@ int cuda_fail(cudaError_t e, const char* where) {
   g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
   return FO_E_CUDA;
 }
+
+}  // namespace
+
+// Error text for the other translation units of the library.
+int fo::set_last_error(int code, const char* what) { return fail(code, what); }
+
+namespace {
 
 const fo::DevTableau kTableaus[2] = {
     // ROS3 (fastode/tableaus.py:70-80)

@@ -306,6 +306,31 @@ int fo_update_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const do
  * integrator. No counterpart in the reference (which never times work). */
 int fo_fp64_fma_rate(double* fma_per_second);
 
+/* Bytes of the static device scratch of fo_solve_static. */
+#define FO_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/*
+ * fo_solve without a workspace and without any device allocation. No
+ * counterpart in the reference: it exists for callers that cannot allocate
+ * device memory while they integrate — a host model that gives the device to
+ * its own memory pool at start-up and forbids allocations afterwards, or a
+ * time step that cannot afford the implicit device synchronization of
+ * cudaMalloc/cudaFree. The caller still passes every input and output (same
+ * meaning as fo_solve); the scratch is one file-scope device array of
+ * FO_STATIC_SCRATCH_BYTES (32 MiB) that every GPU loading the library holds
+ * until the process exits, holding as many groups in flight as fit (a
+ * 210-species / 500-reaction group of 32 cells needs about 4.9 MB, so six at a
+ * time). A mechanism whose single group does not fit is rejected with
+ * FO_E_UNSUPPORTED. The first call on each device looks up the array's device
+ * address and should come before any stream capture. All calls share the array:
+ * calls whose kernels overlap on the GPU race on it, so order them on one
+ * stream.
+ */
+int fo_solve_static(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
+                    int32_t max_group_cells, double* Y, int64_t y_cell_stride, int64_t y_species_stride,
+                    const double* k, int64_t k_cell_stride, int64_t k_reaction_stride, const double* atol,
+                    double rtol, double dt, double* memory, int64_t* counts, int32_t* status, void* stream);
+
 /* Last CUDA error text seen by the library (thread-local, never NULL). */
 const char* fo_last_error(void);
 
