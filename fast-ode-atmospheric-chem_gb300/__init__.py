@@ -10,7 +10,7 @@ integrator.
 from .tableaus import ROS3, RODAS3, Tableau
 from .counts import Counts
 from .chem import Mechanism, ChemSystem
-from .solvers import Algorithm, Memory, RestartingLoop, quantize
+from .solvers import Algorithm, BackwardEuler, Memory, RestartingLoop, quantize
 
-__all__ = ["ROS3", "RODAS3", "Tableau", "Counts", "Mechanism", "ChemSystem", "Algorithm", "RestartingLoop", "Memory",
+__all__ = ["ROS3", "RODAS3", "Tableau", "Counts", "Mechanism", "ChemSystem", "Algorithm", "BackwardEuler", "RestartingLoop", "Memory",
            "quantize"]

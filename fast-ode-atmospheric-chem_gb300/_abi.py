@@ -11,7 +11,9 @@ import threading
 from .build import library_path
 
 FO_OK = 0
-STATUS_STRINGS = ("converged", "too many steps", "step too small", "nan or inf", "projection failed")
+FO_E_INVALID, FO_E_CUDA, FO_E_UNSUPPORTED, FO_E_WORKSPACE, FO_E_ALLOC = -1, -2, -3, -4, -5
+STATUS_STRINGS = ("converged", "too many steps", "step too small", "nan or inf", "projection failed",
+                  "accepted unconverged")
 NUM_COUNTS = 13
 ORDERINGS = {"auto": 0, "natural": 1, "min_degree": 2, "min_fill": 3}
 ORDERING_NAMES = {v: k for k, v in ORDERINGS.items()}
@@ -47,10 +49,13 @@ class Options(C.Structure):
                 ("safety", C.c_double), ("fac_min", C.c_double), ("fac_max", C.c_double),
                 ("carry", C.c_int32), ("quantize", C.c_int32), ("carry_memory", C.c_int32),
                 ("max_steps", C.c_int32), ("variant", C.c_int32), ("loop", C.c_int32),
-                ("step_change_rows", C.c_int32)]
+                ("step_change_rows", C.c_int32),
+                ("max_iterations", C.c_int32), ("nreductions", C.c_int32),
+                ("reductions", C.c_double * 8), ("small", C.c_double)]
 
 
 VARIANTS = {"pipelined": 0, "plain": 1}
+LOOPS = {"algorithm": 0, "restarting": 1, "backward-euler": 2}
 
 
 class BatchDesc(C.Structure):

@@ -3,6 +3,7 @@
 // and the text of the error is kept for fo_last_error().
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
@@ -312,9 +313,21 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
   p.o.carry_memory = opt->carry_memory;
   p.o.max_steps = opt->max_steps;
   p.o.variant = opt->variant;
-  if (opt->loop != FO_LOOP_ALGORITHM && opt->loop != FO_LOOP_RESTARTING) return fail(FO_E_INVALID, "unknown loop");
+  if (opt->loop != FO_LOOP_ALGORITHM && opt->loop != FO_LOOP_RESTARTING && opt->loop != FO_LOOP_BACKWARD_EULER)
+    return fail(FO_E_INVALID, "unknown loop");
   p.o.loop = opt->loop;
   p.o.step_change_rows = opt->step_change_rows;
+  if (opt->loop == FO_LOOP_BACKWARD_EULER) {
+    if (opt->nreductions < 0 || opt->nreductions > 8) return fail(FO_E_INVALID, "nreductions must be 0..8");
+    for (int i = 0; i < opt->nreductions; ++i)
+      if (!(opt->reductions[i] > 0.0) || !std::isfinite(opt->reductions[i]))
+        return fail(FO_E_INVALID, "backward Euler reductions must be positive and finite");
+    if (!std::isfinite(opt->small)) return fail(FO_E_INVALID, "small must be finite");
+    p.o.max_iterations = opt->max_iterations;
+    p.o.nreductions = opt->nreductions;
+    for (int i = 0; i < 8; ++i) p.o.reductions[i] = i < opt->nreductions ? opt->reductions[i] : 1.0;
+    p.o.small = opt->small;
+  }
   // the pipelined kernel needs the packed stream (positions below 65,536 and
   // rows shorter than 32,767 entries); larger mechanisms run the plain loops
   if (p.o.variant == FO_VARIANT_PIPELINED && plan->dev.elp == nullptr) p.o.variant = FO_VARIANT_PLAIN;
@@ -545,6 +558,8 @@ int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngro
   if (mode != 0 && mode != 1) return fail(FO_E_INVALID, "mode must be 0 (replay) or 1 (adjoint)");
   if (mode == 0 && !Yout) return fail(FO_E_INVALID, "replay needs Yout");
   if (mode == 1 && (!lam || !thbar)) return fail(FO_E_INVALID, "adjoint needs lam and thbar");
+  if (opt && opt->loop == FO_LOOP_BACKWARD_EULER)
+    return fail(FO_E_UNSUPPORTED, "the adjoint replays Rosenbrock steps: backward Euler has none");
   fo::AdjParams a;
   std::memset(&a, 0, sizeof(a));
   size_t smem = 0;

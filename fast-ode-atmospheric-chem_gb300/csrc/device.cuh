@@ -56,6 +56,10 @@ struct DevOptions {
   int loop;        // FO_LOOP_*
   int step_change_rows;
   double k_exp;    // embedded order + 1
+  // backward Euler (FO_LOOP_BACKWARD_EULER)
+  int max_iterations, nreductions;
+  double reductions[8];
+  double small;
 };
 
 // Per-lane scratch layout, in items (each item is `lanes` doubles).

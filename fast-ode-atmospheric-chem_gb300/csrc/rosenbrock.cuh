@@ -781,10 +781,134 @@ __device__ __noinline__ void solve_group_restarting(const SolveParams& p, int g,
   }
 }
 
+// The baseline backward Euler, fastode/solvers.py:439-491 statement by
+// statement: every Newton iteration evaluates F and J at the iterate, factors
+// M/H - J and solves for the update; the iterate is clamped at zero after
+// each update. From the second iteration on, the step has converged when
+// every update of the group is finite and within max(small, atol, rtol |Y|).
+// A failed step restarts from the last accepted state with H cut by the next
+// reduction; past the last reduction the unconverged iterate is accepted and
+// the call ends. Two converged steps in a row double H.
+__device__ __noinline__ void solve_group_backward_euler(const SolveParams& p, int g, double* scr, double* w,
+                                                        double* red) {
+  const int L = blockDim.x, lane = threadIdx.x;
+  const int n = p.t.n;
+  const int64_t c0 = p.group_offsets[g], C = p.group_offsets[g + 1] - c0;
+  Lane ln;
+  ln.lane = lane;
+  ln.L = L;
+  ln.active = lane < C;
+  ln.cell = c0 + (ln.active ? lane : (C - 1));
+  const DevOptions& o = p.o;
+  const double dt = p.dt;
+  long long c_steps = 0, c_acc = 0, c_rej = 0, c_rhs = 0, c_jac = 0, c_lu = 0, c_solves = 0;
+  long long c_newton = 0, c_fail = 0, c_unconv = 0;
+  double* Yn = scr + p.sl.y * L;
+  double* Yn1 = scr + p.sl.ynew * L;
+  double* F = scr + p.sl.f0 * L;
+  double* negj = scr + p.sl.negj * L;
+  double* dd = scr + p.sl.d * L;
+  double* rr = scr + p.sl.r * L;
+  double* lu = scr + p.sl.lu * L;
+  for (int i = 0; i < n; ++i) {
+    const double v = p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss];
+    SCR(Yn, i) = v;
+    SCR(Yn1, i) = v;
+  }
+  double H = dt, t = 0.0;
+  int n_success = 0, n_fail = 0;
+  int status = FO_STATUS_CONVERGED;
+  while (t < dt) {
+    if (c_steps >= o.max_steps) {   // a guard of this build: the reference's loop has no budget
+      status = FO_STATUS_TOO_MANY_STEPS;
+      break;
+    }
+    bool ok = false;
+    int iterations = 0;
+    for (;;) {
+      ++c_newton;
+      eval_rhs(p, ln, Yn1, rr, F);
+      ++c_rhs;
+      eval_negjac(p, ln, Yn1, dd, negj);
+      ++c_jac;
+      factor_any(p, ln, 1.0 / H, negj, lu, w, false);
+      ++c_lu;
+      for (int i = 0; i < n; ++i)
+        WROW(i) = __dsub_rn(SCR(F, i), __ddiv_rn(__dsub_rn(SCR(Yn1, i), SCR(Yn, i)), H));
+      solve_in_w(p, ln, lu, w);
+      ++c_solves;
+      ++iterations;
+      bool conv = true;
+      for (int i = 0; i < n; ++i) {
+        const double d = WROW(i);
+        const double y = clamp0(__dadd_rn(SCR(Yn1, i), d));
+        SCR(Yn1, i) = y;
+        if (iterations > 1) {
+          const double bound = npmax(npmax(o.small, __ldg(p.atol + __ldg(p.t.perm + i))), __dmul_rn(p.rtol, fabs(y)));
+          conv = conv && isfinite(d) && fabs(d) <= bound;
+        }
+      }
+      if (iterations > 1) ok = block_all(!ln.active || conv);
+      if (ok || iterations >= o.max_iterations) break;
+    }
+    ++c_steps;
+    if (!ok) {
+      ++c_rej;
+      ++c_fail;
+      n_success = 0;
+      if (n_fail >= o.nreductions) {
+        t = __dadd_rn(t, H);
+        ++c_unconv;
+        status = FO_STATUS_ACCEPTED_UNCONVERGED;
+        bool finite = true;
+        for (int i = 0; i < n; ++i) finite = finite && isfinite(SCR(Yn1, i));
+        if (!block_all(!ln.active || finite)) status = FO_STATUS_NAN_OR_INF;
+        break;
+      }
+      for (int i = 0; i < n; ++i) SCR(Yn1, i) = SCR(Yn, i);
+      H = __dmul_rn(H, o.reductions[n_fail]);
+      ++n_fail;
+    } else {
+      ++c_acc;
+      t = __dadd_rn(t, H);
+      for (int i = 0; i < n; ++i) SCR(Yn, i) = SCR(Yn1, i);
+      ++n_success;
+      if (n_success >= 2) {
+        n_success = 0;
+        H = __dmul_rn(H, 2.0);
+      }
+    }
+    H = pymin(H, __dsub_rn(dt, t));
+  }
+  if (ln.active)
+    for (int i = 0; i < n; ++i) {
+      double y = SCR(Yn1, i);
+      if (!p.t.has_constraints || __ldg(p.t.mass + i) == 1.0) y = clamp0(y);
+      p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss] = y;
+    }
+  if (threadIdx.x == 0) {
+    long long* cn = p.counts + (int64_t)g * FO_NUM_COUNTS;
+    cn[0] += c_steps;
+    cn[1] += c_acc;
+    cn[2] += c_rej;
+    cn[3] += c_rhs;
+    cn[4] += c_jac;
+    cn[5] += c_lu;
+    cn[6] += c_solves;
+    cn[7] += c_newton;
+    cn[8] += c_fail;
+    cn[9] += c_unconv;
+    cn[12] += 1;
+    p.status[g] = status;
+    if (p.trace_len) p.trace_len[g] = 0;
+  }
+}
+
 __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, double* w, double* red);
 
 __device__ void solve_group(const SolveParams& p, int g, double* scr, double* w, double* red) {
   if (p.o.loop == FO_LOOP_RESTARTING) solve_group_restarting(p, g, scr, w, red);
+  else if (p.o.loop == FO_LOOP_BACKWARD_EULER) solve_group_backward_euler(p, g, scr, w, red);
   else solve_group_algorithm(p, g, scr, w, red);
 }
 

@@ -76,6 +76,47 @@ def _k_rows(system, C_cells: int) -> np.ndarray:
     return np.ascontiguousarray(k)
 
 
+def _device_solve(solver, system, Y, dt, atol, rtol, counts: Counts, mem):
+    """One fo_solve call on one group: the host side of every solver's
+    ``solve``. ``mem`` is a Memory updated in place, or None when the loop
+    carries nothing (its device copy is then neither read nor written)."""
+    _require_chem(system)
+    torch = _torch()
+    Y = np.asarray(Y, dtype=np.float64)
+    if Y.ndim != 2:
+        raise ValueError("Y must have shape (cells, species)")
+    C_cells, n = Y.shape
+    if n != system.n:
+        raise ValueError(f"Y has {n} species, the system {system.n}")
+    plan = plan_for(system.mech, system.mass, solver.ordering)
+    k = _k_rows(system, C_cells)
+    atol = np.array(np.broadcast_to(np.asarray(atol, dtype=np.float64), (n,)))
+    dev = torch.device("cuda", plan.device)
+    Yd = torch.from_numpy(np.ascontiguousarray(Y)).to(dev)
+    kd = torch.from_numpy(k).to(dev)
+    atold = torch.from_numpy(atol).to(dev)
+    m = mem if mem is not None else Memory()
+    memd = torch.tensor([m.h_next, m.err_prev, m.h_prev], dtype=torch.float64, device=dev)
+    cnt = torch.zeros((1, _abi.NUM_COUNTS), dtype=torch.int64, device=dev)
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    offs = torch.tensor([0, C_cells], dtype=torch.int32, device=dev)
+    ws = plan.workspace(1, C_cells)
+    stream = torch.cuda.current_stream(dev)
+    rc = _abi.lib().fo_solve(
+        plan.handle, C.byref(solver.options()), 1, offs.data_ptr(), C_cells,
+        Yd.data_ptr(), n, 1, kd.data_ptr(), 0 if k.shape[0] == 1 else plan.R, 1,
+        atold.data_ptr(), float(rtol), float(dt),
+        memd.data_ptr(), cnt.data_ptr(), st.data_ptr(), ws.data_ptr(), ws.numel(), 0,
+        None, 0, None, C.c_void_p(stream.cuda_stream))
+    _abi.check(rc, "fo_solve")
+    stream.synchronize()
+    if mem is not None:
+        h = memd.cpu().numpy()
+        mem.h_next, mem.err_prev, mem.h_prev = float(h[0]), float(h[1]), float(h[2])
+    counts.add_row(cnt.cpu().numpy()[0])
+    return Yd.cpu().numpy(), _abi.STATUS_STRINGS[int(st.cpu().item())]
+
+
 class Algorithm:
     """The integrator of the reference's Section 4 (fastode/solvers.py:270-415)."""
 
@@ -127,40 +168,8 @@ class Algorithm:
         """Integrate one group (all rows of Y) over one interval; returns
         (Y_new, status). Y is copied, ``counts`` accumulated and ``memory``
         updated in place, as in the reference."""
-        _require_chem(system)
-        torch = _torch()
-        Y = np.asarray(Y, dtype=np.float64)
-        if Y.ndim != 2:
-            raise ValueError("Y must have shape (cells, species)")
-        C_cells, n = Y.shape
-        if n != system.n:
-            raise ValueError(f"Y has {n} species, the system {system.n}")
-        plan = plan_for(system.mech, system.mass, self.ordering)
-        k = _k_rows(system, C_cells)
-        atol = np.array(np.broadcast_to(np.asarray(atol, dtype=np.float64), (n,)))
-        mem = memory if memory is not None else Memory()
-        dev = torch.device("cuda", plan.device)
-        Yd = torch.from_numpy(np.ascontiguousarray(Y)).to(dev)
-        kd = torch.from_numpy(k).to(dev)
-        atold = torch.from_numpy(atol).to(dev)
-        memd = torch.tensor([mem.h_next, mem.err_prev, mem.h_prev], dtype=torch.float64, device=dev)
-        cnt = torch.zeros((1, _abi.NUM_COUNTS), dtype=torch.int64, device=dev)
-        st = torch.zeros(1, dtype=torch.int32, device=dev)
-        offs = torch.tensor([0, C_cells], dtype=torch.int32, device=dev)
-        ws = plan.workspace(1, C_cells)
-        stream = torch.cuda.current_stream(dev)
-        rc = _abi.lib().fo_solve(
-            plan.handle, C.byref(self.options()), 1, offs.data_ptr(), C_cells,
-            Yd.data_ptr(), n, 1, kd.data_ptr(), 0 if k.shape[0] == 1 else plan.R, 1,
-            atold.data_ptr(), float(rtol), float(dt),
-            memd.data_ptr(), cnt.data_ptr(), st.data_ptr(), ws.data_ptr(), ws.numel(), 0,
-            None, 0, None, C.c_void_p(stream.cuda_stream))
-        _abi.check(rc, "fo_solve")
-        stream.synchronize()
-        h = memd.cpu().numpy()
-        mem.h_next, mem.err_prev, mem.h_prev = float(h[0]), float(h[1]), float(h[2])
-        counts.add_row(cnt.cpu().numpy()[0])
-        return Yd.cpu().numpy(), _abi.STATUS_STRINGS[int(st.cpu().item())]
+        return _device_solve(self, system, Y, dt, atol, rtol, counts,
+                             memory if memory is not None else Memory())
 
 
 class RestartingLoop(Algorithm):
@@ -188,7 +197,67 @@ class RestartingLoop(Algorithm):
 
     def solve(self, system, Y, dt, atol, rtol, counts: Counts, memory=None):
         """Integrate one group over one interval; returns (Y_new, status)."""
-        return super().solve(system, Y, dt, atol, rtol, counts, None)
+        return _device_solve(self, system, Y, dt, atol, rtol, counts, None)
+
+
+class BackwardEuler:
+    """The baseline backward Euler with a full Newton iteration
+    (fastode/solvers.py:418-491) on the GPU: every Newton iteration evaluates
+    the rhs and Jacobian, factors M/H - J and solves once; a failed step is
+    retried from the last accepted state with H cut by the next reduction,
+    and past the last reduction the unconverged iterate is accepted
+    ("accepted unconverged"). Counts newton, failures and unconverged as the
+    reference does. ``max_steps`` is a guard the reference does not have (its
+    loop has no budget): a group that takes more steps in one call reports
+    "too many steps". ``ordering`` and ``kernel`` choose the device LU as for
+    Algorithm."""
+
+    name = "backward-euler"
+
+    def __init__(self, max_iterations: int = 11, reductions=(0.5, 0.5, 0.5, 0.5, 0.1),
+                 small: float = 1.0e-40, max_steps: int = 1_000_000, ordering: str = "auto",
+                 kernel: str = "pipelined"):
+        self.max_iterations = max_iterations
+        self.reductions = tuple(float(r) for r in reductions)
+        if len(self.reductions) > 8:
+            raise ValueError("the device loop takes at most 8 reductions")
+        if not all(r > 0.0 and math.isfinite(r) for r in self.reductions):
+            raise ValueError("reductions must be positive and finite")
+        self.small = small
+        self.max_steps = max_steps
+        self.ordering = ordering
+        if kernel not in _abi.VARIANTS:
+            raise ValueError(f"kernel must be one of {sorted(_abi.VARIANTS)}")
+        self.kernel = kernel
+
+    def new_memory(self):
+        return None
+
+    def converged(self, delta, Y, atol, rtol) -> bool:
+        """The Newton convergence test (fastode/solvers.py:432-437), as the
+        device applies it to every iterate of a group."""
+        if not np.all(np.isfinite(delta)):
+            return False
+        bound = np.maximum(np.maximum(self.small, np.asarray(atol)[None, :]), rtol * np.abs(Y))
+        return bool(np.all(np.abs(delta) <= bound))
+
+    def options(self) -> _abi.Options:
+        o = _abi.Options()
+        o.tableau = 0
+        o.controller = 1
+        o.max_steps = int(self.max_steps)
+        o.variant = _abi.VARIANTS[self.kernel]
+        o.loop = _abi.LOOPS["backward-euler"]
+        o.max_iterations = int(self.max_iterations)
+        o.nreductions = len(self.reductions)
+        for i, r in enumerate(self.reductions):
+            o.reductions[i] = r
+        o.small = float(self.small)
+        return o
+
+    def solve(self, system, Y, dt, atol, rtol, counts: Counts, memory=None):
+        """Integrate one group over one interval; returns (Y_new, status)."""
+        return _device_solve(self, system, Y, dt, atol, rtol, counts, None)
 
 
 def _eval(system, Y, jac: bool):

@@ -44,6 +44,7 @@ extern "C" {
 #define FO_STATUS_STEP_TOO_SMALL 2     /* "step too small" */
 #define FO_STATUS_NAN_OR_INF 3         /* "nan or inf" */
 #define FO_STATUS_PROJECTION_FAILED 4  /* "projection failed" */
+#define FO_STATUS_ACCEPTED_UNCONVERGED 5  /* "accepted unconverged" (backward Euler, fastode/solvers.py:470-478) */
 
 /* Number and order of the per-group counters (fastode/counts.py:10-23):
  * steps, accepted, rejected, rhs, jac, lu, solves, newton, failures,
@@ -119,6 +120,12 @@ typedef struct fo_options {
   int32_t loop;               /* FO_LOOP_*: the step loop */
   int32_t step_change_rows;   /* restarting loop with constraints: the step change replaces the
                                  algebraic rows of the error estimate (fastode/solvers.py:194-200) */
+  /* Backward Euler (FO_LOOP_BACKWARD_EULER): the constructor arguments of
+   * fastode.solvers.BackwardEuler (fastode/solvers.py:418-430). */
+  int32_t max_iterations;     /* Newton iterations per step (11) */
+  int32_t nreductions;        /* entries of reductions used, 0..8 (5) */
+  double reductions[8];       /* step factor after the i-th failed step (0.5, 0.5, 0.5, 0.5, 0.1); each > 0 */
+  double small;               /* floor of the convergence bound (1e-40) */
 } fo_options;
 
 /* Step loops. ALGORITHM is fastode.solvers.Algorithm (fastode/solvers.py:270-415);
@@ -128,6 +135,19 @@ typedef struct fo_options {
  * memory array are ignored; the memory array is neither read nor written). */
 #define FO_LOOP_ALGORITHM 0
 #define FO_LOOP_RESTARTING 1
+/* BACKWARD_EULER is the baseline fastode.solvers.BackwardEuler
+ * (fastode/solvers.py:418-491): backward Euler with a full Newton iteration
+ * (rhs, Jacobian, factorization of M/H - J and one solve per iteration), the
+ * step cut by reductions[i] after the i-th failed Newton iteration and doubled
+ * after two converged steps in a row; past nreductions failures the last
+ * iterate is accepted and the group reports FO_STATUS_ACCEPTED_UNCONVERGED.
+ * It uses max_iterations, nreductions, reductions, small and max_steps; the
+ * tableau must still name a valid tableau (it is not used), and the memory
+ * array is neither read nor written. max_steps has no counterpart in the
+ * reference, whose loop has no budget: it only guards against step
+ * sequences that would not end (a group past it reports
+ * FO_STATUS_TOO_MANY_STEPS). */
+#define FO_LOOP_BACKWARD_EULER 2
 
 /* Kernel variants of the factorization and solves. PIPELINED streams the
  * elimination schedule with register double-buffering (the fast path);

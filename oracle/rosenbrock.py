@@ -475,6 +475,76 @@ class OAlgorithm:
         return clamp(system, Y), status
 
 
+@dataclass
+class OBackwardEuler:
+    """fastode/solvers.py:418-491, statement by statement."""
+    max_iterations: int = 11
+    reductions: tuple = (0.5, 0.5, 0.5, 0.5, 0.1)
+    small: float = 1.0e-40
+
+    def new_memory(self):
+        return None
+
+    def converged(self, delta, Y, atol, rtol):     # solvers.py:432-437
+        if not np.all(np.isfinite(delta)):
+            return False
+        bound = np.maximum(np.maximum(self.small, atol[None, :]), rtol * np.abs(Y))
+        return bool(np.all(np.abs(delta) <= bound))
+
+    def solve(self, system, Y, dt, atol, rtol, counts, memory=None):   # solvers.py:439-491
+        counts.calls += 1
+        H = dt
+        t = 0.0
+        n_success = n_fail = 0
+        Yn = Y.copy()
+        Yn1 = Y.copy()
+        status = "converged"
+        while t < dt:
+            ok = False
+            iterations = 0
+            while True:
+                counts.newton += 1
+                F = system.rhs(Yn1)
+                counts.rhs += 1
+                J = system.jac(Yn1)
+                counts.jac += 1
+                LU = system.factor(1.0 / H, J)
+                counts.lu += 1
+                delta = LU.solve(F - (Yn1 - Yn) / H)
+                counts.solves += 1
+                Yn1 = np.maximum(Yn1 + delta, 0.0)
+                iterations += 1
+                if iterations > 1:
+                    ok = self.converged(delta, Yn1, atol, rtol)
+                if ok or iterations >= self.max_iterations:
+                    break
+            counts.steps += 1
+            if not ok:
+                counts.rejected += 1
+                counts.failures += 1
+                n_success = 0
+                if n_fail >= len(self.reductions):
+                    t += H
+                    counts.unconverged += 1
+                    status = "accepted unconverged"
+                    if not np.all(np.isfinite(Yn1)):
+                        status = "nan or inf"
+                    break
+                Yn1 = Yn.copy()
+                H *= self.reductions[n_fail]
+                n_fail += 1
+            else:
+                counts.accepted += 1
+                t += H
+                Yn = Yn1.copy()
+                n_success += 1
+                if n_success >= 2:
+                    n_success = 0
+                    H *= 2.0
+            H = min(H, dt - t)
+        return clamp(system, Yn1), status
+
+
 def fixed_steps(system, tab, Y, t_end, n_steps, counts=None):   # solvers.py:494-504
     counts = counts or OCounts()
     H = t_end / n_steps
@@ -489,11 +559,13 @@ def fixed_steps(system, tab, Y, t_end, n_steps, counts=None):   # solvers.py:494
 # ---- a scenario loop over groups and intervals (fastode/ts1.py:181-223 pattern) -------
 
 def run_groups(mech, Y0, k_at, dt, intervals, atol, rtol, group_size=32, tableau=OROS3,
-               mass=None, groups=None, trace=False, **alg_kw):
+               mass=None, groups=None, trace=False, solver=None, **alg_kw):
     """Integrate the cells of Y0 (C, n) in groups over `intervals` intervals,
     each group with its own memory; k_at(i) gives the (C, R) rate constants of
-    interval i. Returns (Y, counts per group, statuses per group and interval,
-    memory per group, traces per group)."""
+    interval i. `solver`, when given, makes each group's solver (for example
+    OBackwardEuler); the default is OAlgorithm(tableau, **alg_kw). Returns (Y,
+    counts per group, statuses per group and interval, memory per group,
+    traces per group)."""
     C = Y0.shape[0]
     starts = list(range(0, C, group_size))
     if groups is not None:
@@ -503,8 +575,8 @@ def run_groups(mech, Y0, k_at, dt, intervals, atol, rtol, group_size=32, tableau
     ks = [k_at(i) for i in range(intervals)]
     for g0 in starts:
         sl = slice(g0, min(g0 + group_size, C))
-        alg = OAlgorithm(tableau=tableau, trace=[] if trace else None, **alg_kw)
-        mem = OMemory()
+        alg = solver() if solver is not None else OAlgorithm(tableau=tableau, trace=[] if trace else None, **alg_kw)
+        mem = alg.new_memory() if solver is not None else OMemory()
         c = OCounts()
         st = []
         Yg = Y[sl].copy()
@@ -516,7 +588,7 @@ def run_groups(mech, Y0, k_at, dt, intervals, atol, rtol, group_size=32, tableau
         counts.append(c)
         statuses.append(st)
         memories.append(mem)
-        traces.append(alg.trace)
+        traces.append(getattr(alg, "trace", None))
     return Y, counts, statuses, memories, traces
 
 

@@ -220,14 +220,72 @@ def ts1_case(reference):
                 n_failed=len(statuses))
 
 
+# BackwardEuler on TS1 tier1-30s: the three archived configurations
+# (experiments/ts1_experiments.py:60-61; Counts checked against
+# reference-results/ts1/runs.csv) and two that make the Newton iteration fail,
+# so that step cuts, doubling after two successes and accepted unconverged
+# iterates all occur. name: (constructor arguments, rtol, atol, archived).
+BE_CONFIGS = {
+    "be": ({}, 1e-6, 1e-3, True),
+    "be_tight_3": ({}, 1e-3, 1e-15, True),
+    "be_tight_6": ({}, 1e-6, 1e-15, True),
+    "be_it2": ({"max_iterations": 2}, 1e-6, 1e-15, False),
+    "be_it3": ({"max_iterations": 3, "reductions": (0.5, 0.25)}, 1e-8, 1e-18, False),
+}
+BE_STATUS = {"converged": 0, "nan or inf": 3, "accepted unconverged": 5}
+
+
+def backward_euler_ts1(reference):
+    """Final states, Counts and per-interval statuses of the reference's
+    BackwardEuler through run_scenario on TS1 tier1-30s (the inputs are those
+    of ts1_tier1_30s.npz)."""
+    import csv
+    from fastode import BackwardEuler
+    from fastode.ts1 import TS1, Cells, Scenario, run_scenario
+
+    ts1 = TS1()
+    sc = Scenario(Path(reference) / "data/scenarios/tier1-30s/scenario.txt")
+    cells = Cells(ts1, sc.cells)
+    out = {}
+    for name, (kw, rtol, atol, archived) in BE_CONFIGS.items():
+        snaps, counts, failed = run_scenario(sc, BackwardEuler(**kw), cells, ts1, rtol, atol)
+        if archived:
+            config = "be" if name == "be" else "be-tight"
+            with open(Path(reference) / "reference-results/ts1/runs.csv") as fh:
+                row = next(r for r in csv.DictReader(fh) if r["config"] == config and r["scenario"] == "tier1-30s"
+                           and float(r["rtol"]) == rtol and float(r["atol"]) == atol)
+            for field in ("steps", "accepted", "rejected", "rhs", "jac", "lu", "solves", "newton", "failures",
+                          "unconverged"):
+                assert int(row[field]) == getattr(counts, field), (name, field)
+        ngroups = (cells.C + 31) // 32
+        status = np.zeros((ngroups, sc.steps), dtype=np.int32)
+        for g0, i, st in failed:          # (first cell of the group, interval, status)
+            status[g0 // 32, i] = BE_STATUS[st]
+        out[f"{name}_Y"] = snaps[sc.steps]
+        out[f"{name}_counts"] = np.array(list(counts.as_dict().values()))
+        out[f"{name}_tol"] = np.array([rtol, atol])
+        out[f"{name}_max_iterations"] = np.array(kw.get("max_iterations", 11))
+        out[f"{name}_reductions"] = np.array(kw.get("reductions", (0.5, 0.5, 0.5, 0.5, 0.1)))
+        out[f"{name}_status"] = status
+        print(name, list(counts.as_dict().values()), len(failed), "non-converged group-intervals")
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", choices=["backward-euler"], default=None,
+                    help="regenerate one fixture instead of all")
     a = ap.parse_args()
     sys.path.insert(0, a.reference)
     sys.path.insert(0, str(ROOT))
     import fastode
     from fastode_gb300 import synthetic as syn
+
+    if a.only == "backward-euler":
+        np.savez_compressed(HERE / "ts1_tier1_30s_backward_euler.npz", **backward_euler_ts1(a.reference))
+        return
+    np.savez_compressed(HERE / "ts1_tier1_30s_backward_euler.npz", **backward_euler_ts1(a.reference))
 
     ts1 = ts1_case(a.reference)
     np.savez_compressed(HERE / "ts1_tier1_30s.npz", **ts1)

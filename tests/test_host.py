@@ -153,3 +153,54 @@ def test_analysis_rejects_bad_descriptors(built_library):
     rc = _abi.lib().fo_analyze(ctypes.byref(d.desc), 0, ctypes.byref(info), None)
     assert rc == -1
     assert b"out of range" in _abi.lib().fo_last_error()
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes structures of the binding have the offsets and sizes the C
+    compiler gives the header's structs (compiled here with the host gcc)."""
+    import shutil
+    import subprocess
+    from fastode_gb300 import _abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    structs = {"fo_options": _abi.Options, "fo_batch_desc": _abi.BatchDesc,
+               "fo_mechanism_desc": _abi.MechanismDesc, "fo_plan_info": _abi.PlanInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fastode_gb300.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for field, _ in cls._fields_:
+            lines.append(f'  printf("{cname}.{field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    for cname, cls in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(cls), cname
+        for field, _ in cls._fields_:
+            assert int(got[f"{cname}.{field}"]) == getattr(cls, field).offset, (cname, field)
+
+
+def test_backward_euler_options_and_validation():
+    """BackwardEuler keeps the reference's constructor defaults
+    (fastode/solvers.py:423-427) and maps them onto fo_options."""
+    from fastode_gb300 import BackwardEuler, _abi
+    be = BackwardEuler()
+    assert be.name == "backward-euler" and be.new_memory() is None
+    o = be.options()
+    assert o.loop == _abi.LOOPS["backward-euler"] and o.max_iterations == 11
+    assert o.nreductions == 5 and list(o.reductions)[:5] == [0.5, 0.5, 0.5, 0.5, 0.1]
+    assert o.small == 1.0e-40
+    with pytest.raises(ValueError):
+        BackwardEuler(reductions=(0.5, 0.0))
+    with pytest.raises(ValueError):
+        BackwardEuler(reductions=(0.5,) * 9)
+    # the convergence test of fastode/solvers.py:432-437
+    Y = np.array([[1.0, 1e-30]])
+    atol = np.array([1e-12, 1e-12])
+    assert be.converged(np.array([[1e-7, 1e-13]]), Y, atol, 1e-6)
+    assert not be.converged(np.array([[1e-5, 0.0]]), Y, atol, 1e-6)
+    assert not be.converged(np.array([[np.nan, 0.0]]), Y, atol, 1e-6)

@@ -207,3 +207,28 @@ def test_oracle_reproduces_ts1_tier1_archive():
     total = np.sum([c.as_tuple() for c in counts], axis=0)
     np.testing.assert_array_equal(total, f["counts"])
     np.testing.assert_array_equal(Y, f["Y"])
+
+
+@pytest.mark.parametrize("config", ["be_tight_6", "be_it3"])
+def test_oracle_backward_euler_reproduces_ts1_reference(config):
+    """BackwardEuler (fastode/solvers.py:418-491) on TS1 tier1-30s through the
+    oracle: the reference's final states bit for bit, its Counts (for
+    be_tight_6 the archived row of reference-results/ts1/runs.csv: 616 Newton
+    iterations over 202 steps) and its per-interval statuses. be_it3 makes
+    the Newton iteration fail, so step cuts and accepted unconverged iterates
+    occur."""
+    from golden_cases import table_mechanism, ts1_k
+    f = load("ts1_tier1_30s")
+    b = load("ts1_tier1_30s_backward_euler")
+    mech = table_mechanism(f)
+    rtol, atol = b[f"{config}_tol"]
+    make = lambda: O.OBackwardEuler(max_iterations=int(b[f"{config}_max_iterations"]),  # noqa: E731
+                                    reductions=tuple(b[f"{config}_reductions"]))
+    Y, counts, statuses, _, _ = O.run_groups(mech, f["Y0"], lambda i: ts1_k(f, i), float(f["dt"]),
+                                             int(f["intervals"]), np.full(mech.n, atol), float(rtol),
+                                             group_size=32, solver=make)
+    total = np.sum([c.as_tuple() for c in counts], axis=0)
+    np.testing.assert_array_equal(total, b[f"{config}_counts"])
+    codes = {"converged": 0, "nan or inf": 3, "accepted unconverged": 5}
+    np.testing.assert_array_equal(np.array([[codes[s] for s in st] for st in statuses]), b[f"{config}_status"])
+    np.testing.assert_array_equal(Y, b[f"{config}_Y"])
