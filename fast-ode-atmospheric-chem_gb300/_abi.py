@@ -56,6 +56,7 @@ class Options(C.Structure):
 
 VARIANTS = {"pipelined": 0, "plain": 1}
 LOOPS = {"algorithm": 0, "restarting": 1, "backward-euler": 2}
+SCORE_RULES = {"ts1": 0, "digits": 1}
 
 
 class BatchDesc(C.Structure):
@@ -91,6 +92,9 @@ SIGNATURES = {
     "fo_rate_constants": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
     "fo_update_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _D, _P, _I64, _I64, _P]),
     "fo_fp64_fma_rate": (C.c_int, [C.POINTER(C.c_double)]),
+    "fo_scale_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _P, _I64, _I64, _P]),
+    "fo_score_accumulate": (C.c_int, [_I32, _I32, _P, _I64, _I64, _I32, _P, _P, _I64, _I64, _D, _I32,
+                                      _P, _P, _P, _P]),
     "fo_multi_workspace_bytes": (C.c_int, [_I32, C.POINTER(BatchDesc), _I32, C.POINTER(C.c_size_t)]),
     "fo_multi_prepare": (C.c_int, [_I32, C.POINTER(BatchDesc), _P, C.c_size_t, _I32, C.POINTER(_P)]),
     "fo_multi_launch": (C.c_int, [_P, _P]),

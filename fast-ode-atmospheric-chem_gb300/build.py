@@ -19,7 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libfastode_gb300.so"
-SOURCES = ["integrator.cu", "adjoint.cu", "abi.cu", "utility.cu", "static_scratch.cu", "symbolic.cpp"]
+SOURCES = ["integrator.cu", "adjoint.cu", "abi.cu", "utility.cu", "scoring.cu", "static_scratch.cu", "symbolic.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

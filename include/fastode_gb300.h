@@ -321,6 +321,42 @@ int fo_update_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const do
                          const double* phase, double omega, double t, double* k,
                          int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
 
+/* Photolysis columns of one interval of a TS1 scenario:
+ * k(c, rxn[p]) = (base[p * C + c] * factor) * scaling[p], the per-interval
+ * patch of fastode/ts1.py:204-214 (run_scenario sets params[name] = base * f
+ * and then k[:, j] = params[name] * scaling factor). rxn, base (nphoto x C,
+ * cells fastest), scaling (nphoto) and k are device pointers; asynchronous. */
+int fo_scale_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const double* base, const double* scaling,
+                        double factor, double* k, int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
+
+/* Sample rules of the accuracy score. TS1 is fastode.ts1.score
+ * (fastode/ts1.py:252-253): a sample is skipped when ref < threshold (a NaN
+ * reference is counted). DIGITS is fastode.reference.digits
+ * (fastode/reference.py:49): a sample is kept when ref >= threshold. */
+#define FO_SCORE_TS1 0
+#define FO_SCORE_DIGITS 1
+
+/*
+ * The sums behind Sandu's digits (fastode/ts1.py:226-264,
+ * fastode/reference.py:41-59) for one snapshot of C cells, accumulated into
+ * device arrays: for every reference column j with species[j] >= 0 and every
+ * cell c whose reference value r = ref(c, j) is a sample under `rule`,
+ *     sums[j] += ((Y(c, species[j]) - r) / r)^2,   counts[j] += 1.
+ * Digits are then min(16, -log10(sqrt(sum / count))) per column and over all
+ * columns (16 when the mean is <= 0). When gate is not NULL it is set to 0 if
+ * any of the n species of any cell of Y is non-finite or below -1e-20
+ * (fastode/ts1.py:240-241); it is never set to 1, so start it at 1.
+ * Element (c, s) of Y is Y[c * y_cell_stride + s * y_species_stride] and
+ * element (c, j) of ref is ref[c * ref_cell_stride + j * ref_column_stride].
+ * species (m), ref, sums (m), counts (m), gate: device. Each column is
+ * reduced by one block in a fixed order: the sums are reproducible bit for
+ * bit. Asynchronous on `stream`.
+ */
+int fo_score_accumulate(int32_t C, int32_t n, const double* Y, int64_t y_cell_stride, int64_t y_species_stride,
+                        int32_t m, const int32_t* species, const double* ref, int64_t ref_cell_stride,
+                        int64_t ref_column_stride, double threshold, int32_t rule, double* sums, int64_t* counts,
+                        int32_t* gate, void* stream);
+
 /* FP64 fused multiply-add throughput of the current device (FMA per second),
  * measured with a full-warp DFMA kernel: the roofline denominator for the
  * integrator. No counterpart in the reference (which never times work). */

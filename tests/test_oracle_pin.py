@@ -232,3 +232,42 @@ def test_oracle_backward_euler_reproduces_ts1_reference(config):
     codes = {"converged": 0, "nan or inf": 3, "accepted unconverged": 5}
     np.testing.assert_array_equal(np.array([[codes[s] for s in st] for st in statuses]), b[f"{config}_status"])
     np.testing.assert_array_equal(Y, b[f"{config}_Y"])
+
+
+REFERENCE = __import__("pathlib").Path("/root/reference")
+# fixture state -> the archived row of reference-results/ts1/runs.csv it was made with
+SCORED = {
+    ("ts1_tier1_30s", "Y"): ("alg", 1e-3),
+    ("ts1_tier1_30s", "restart_Y"): ("restart", 1e-3),
+    ("ts1_tier1_30s", "alg_elementary_Y"): ("alg-elementary", 5e-4),
+    ("ts1_tier1_30s", "alg_noquant_Y"): ("alg-noquant", 5e-4),
+    ("ts1_tier1_30s_backward_euler", "be_Y"): ("be", 1e-6),
+    ("ts1_tier1_30s_backward_euler", "be_tight_3_Y"): ("be-tight", 1e-3),
+}
+
+
+@pytest.mark.skipif(not REFERENCE.exists(), reason="reference checkout not present")
+@pytest.mark.parametrize("state", sorted(SCORED))
+def test_oracle_score_reproduces_archived_digits(state):
+    """The oracle's score (fastode/ts1.py:226-264) of the reference's final
+    states on tier1-30s against the scenario's MICM reference table gives the
+    archived digits, worst species, worst digits, gate and levels of
+    reference-results/ts1/runs.csv (experiments/ts1_experiments.py:101-111)."""
+    import csv
+    import sys
+    from oracle import scoring as OS
+    sys.path.insert(0, str(REFERENCE))
+    from fastode.ts1 import TS1
+    species = TS1().species
+    fixture, key = state
+    config, rtol = SCORED[state]
+    Y = load(fixture)[key]
+    table = REFERENCE / "data/scenarios/tier1-30s/reference_final.csv"
+    D, per, gate = OS.score({101: Y}, range(64), species, table)
+    ws, wd, l2, l3 = OS.levels(D, per, gate)
+    with open(REFERENCE / "reference-results/ts1/runs.csv") as fh:
+        row = next(r for r in csv.DictReader(fh)
+                   if r["config"] == config and r["scenario"] == "tier1-30s" and float(r["rtol"]) == rtol)
+    assert round(D, 4) == float(row["digits"])
+    assert ws == row["worst_species"] and round(wd, 4) == float(row["worst_digits"])
+    assert (str(gate), str(l2), str(l3)) == (row["gate"], row["level2"], row["level3"])
