@@ -36,6 +36,15 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "cell-intervals/s at rtol=1e-3 on 1 GB300 vs plain GPU + CPU ref; adjoint/forward cost"
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
+# FLOP of the integrator kernel on this workload, from one ncu capture of the
+# first two timed launches of `bench.py --steps 2 --warmup 3 --no-cpu
+# --e2e-steps 0 --plain-steps 0` (6.589 TB over 1.567 PFLOP). The traffic of a
+# launch is dominated by the elimination's U operands, 8 bytes per 2-FLOP
+# update, so it scales with the algorithmic FLOPs; the bench reports this
+# ratio times its own FLOPs per launch.
+DRAM_BYTES_PER_FLOP = 4.205
+
 
 # ---- CPU baseline: the oracle in a spawn pool, one group per worker --------------------
 
@@ -275,7 +284,10 @@ def run_ours(args, rank, world):
             "attempts": float(counts[:, 0].sum() / len(counts) / args.steps),
             "rejected": float(counts[:, 2].sum() / len(counts) / args.steps)},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": DRAM_BYTES_PER_FLOP * flops / args.steps,
+                     "traffic_unit": "bytes per launch",
+                     "traffic_source": "ncu DRAM bytes per algorithmic FLOP of this kernel on this workload "
+                                       f"({DRAM_BYTES_PER_FLOP} B/FLOP) times this run's FLOPs per launch",
                      "kernel": "solve_kernel", "kernel_ms_per_launch": sum(solve_ms) / len(solve_ms),
                      "peak_source": "fo_fp64_fma_rate: full-warp DFMA kernel, same GPU, same run (the driver's "
                                     "peaks file holds HBM and bf16 only)",
@@ -410,7 +422,7 @@ def run_adjoint(args):
 
     checks = []
     h = 1e-6
-    for d in range(2):
+    for d in range(args.fd_directions):
         dth = rng.standard_normal(wl.sm.R)
         sc = [torch.from_numpy(np.exp(s * h * dth)).to(dev)[:, None] for s in (1.0, -1.0)]
         fd = (loss(A.replay(traj, ks=[k * sc[0] for k in ks])) - loss(A.replay(traj, ks=[k * sc[1] for k in ks]))) / (2 * h)
@@ -420,7 +432,98 @@ def run_adjoint(args):
             "forward_s": t_fwd, "forward_plus_adjoint_s": t_fa, "max_steps_per_interval": traj.max_steps,
             "config": {"workload": f"adjoint ROS3 210x500, {args.cells} cells, {args.steps} x 30 s, "
                                    "gradients w.r.t. 500 log rate constants and the initial state"},
-            "fd_checks": checks}
+            "fd_checks": checks,
+            "fd_max_rel": max((c["rel"] for c in checks), default=None)}
+
+
+def run_dae(args):
+    """Constrained workload: RODAS3 on 150 differential + 10 algebraic species
+    (mass = 0 rows, quasi-steady state), 16,384 cells in groups of 32, 60 s
+    intervals, rtol 1e-4, the projection at every call. Forward throughput
+    (device-resident, CUDA events around the timed intervals), then the
+    adjoint cost ratio on the same run ((forward recorded + adjoint) / plain
+    forward, wall clock) with central-difference checks of the gradient. The
+    adjoint differentiates the Rosenbrock steps with the recorded step sizes;
+    the projection at each interval start is not differentiated (it moves an
+    already consistent state by roundoff only)."""
+    import torch
+    from fastode_gb300 import Algorithm, RODAS3, adjoint as A, build as fbuild, synthetic as syn
+    from fastode_gb300.batch import Batch
+    fbuild.build()
+    dev = torch.device("cuda", 0)
+    wl = syn.dae_constrained(n_cells=args.cells, intervals=args.steps + args.warmup)
+    ks = [torch.from_numpy(np.ascontiguousarray(wl.k_at(i).T)).to(dev) for i in range(args.steps + args.warmup)]
+    atol = torch.from_numpy(wl.atol).to(dev)
+    b = Batch(wl.sm.mech, wl.cells.Y0, group_size=32, algorithm=Algorithm(RODAS3), mass=wl.mass)
+    for i in range(args.warmup):
+        b.step(ks[i], wl.dt, atol, wl.rtol)
+    torch.cuda.synchronize()
+    b.counts.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clocks:
+        e0.record()
+        for i in range(args.steps):
+            b.step(ks[args.warmup + i], wl.dt, atol, wl.rtol)
+        e1.record()
+        torch.cuda.synchronize()
+    s = e0.elapsed_time(e1) / 1e3
+    statuses = b.statuses()
+    c = b.counts.cpu().numpy()
+    out = {"metric": METRIC, "value": wl.cells.C * args.steps / s, "unit": "cell-intervals/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": s / args.steps * 1e3,
+           "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded generator)",
+           "config": {"workload": f"rodas3-dae 150+10 algebraic / 340 reactions, {wl.cells.C} cells in groups "
+                                  f"of 32, dt=60 s, rtol=1e-4, projection every call"},
+           "gpu_launches": args.steps, "statuses": {t: statuses.count(t) for t in set(statuses)},
+           "counts_per_group_interval": {"attempts": float(c[:, 0].sum() / len(c) / args.steps),
+                                         "projection_passes": float(c[:, 10].sum() / len(c) / args.steps)},
+           "clocks": clocks.summary()}
+    if args.adjoint_intervals > 0:
+        m = args.adjoint_intervals
+        Y0 = b.Y.t().contiguous()
+        kk = ks[args.warmup:args.warmup + m]
+        alg = Algorithm(RODAS3)
+
+        def forward():
+            fb = Batch(wl.sm.mech, Y0, group_size=32, algorithm=alg, mass=wl.mass)
+            for i in range(m):
+                fb.step(kk[i], wl.dt, atol, wl.rtol)
+            return fb
+
+        forward()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        forward()
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        traj = A.forward_record(wl.sm.mech, Y0, lambda i: kk[i], wl.dt, wl.atol, wl.rtol, m, algorithm=alg,
+                                mass=wl.mass)
+        Y = traj.batch.Y
+        a = 1e-14
+        target = (Y * 1.01).clone()
+        lam = 2.0 * (torch.log(Y + a) - torch.log(target + a)) / (Y + a)
+        lam0, thbar = A.adjoint(traj, lam)
+        torch.cuda.synchronize()
+        t_fa = time.perf_counter() - t0
+        g_th = thbar.sum(dim=1).cpu().numpy()
+        rng = np.random.default_rng(13)
+
+        def loss(Yend):
+            return float(((torch.log(Yend + a) - torch.log(target + a)) ** 2).sum())
+
+        checks = []
+        for d in range(args.fd_directions):
+            dth = rng.standard_normal(wl.sm.R)
+            sc = [torch.from_numpy(np.exp(sg * 1e-6 * dth)).to(dev)[:, None] for sg in (1.0, -1.0)]
+            fd = (loss(A.replay(traj, ks=[k * sc[0] for k in kk])) -
+                  loss(A.replay(traj, ks=[k * sc[1] for k in kk]))) / 2e-6
+            adj = float(np.dot(g_th, dth))
+            checks.append({"fd": fd, "adjoint": adj, "rel": abs(fd - adj) / max(abs(fd), 1e-300)})
+        out["adjoint"] = {"metric": "adjoint/forward cost", "value": t_fa / t_fwd, "unit": "ratio",
+                          "intervals": m, "forward_s": t_fwd, "forward_plus_adjoint_s": t_fa,
+                          "fd_checks": checks, "fd_max_rel": max((c["rel"] for c in checks), default=None)}
+    return out
 
 
 def run_reference(args, rank, world):
@@ -467,16 +570,22 @@ def main():
     ap.add_argument("--cpu-intervals", type=int, default=30)
     ap.add_argument("--cpu-workers", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint", "dae"],
                     help="plain: the 210/500 drop-in workload (default, the headline line); batched: the "
-                         "three-mechanism persistent launch; adjoint: forward+adjoint cost")
+                         "three-mechanism persistent launch; adjoint: forward+adjoint cost; dae: the RODAS3 "
+                         "constrained workload with its adjoint cost")
+    ap.add_argument("--fd-directions", type=int, default=2,
+                    help="central-difference directions checking the adjoint gradient")
+    ap.add_argument("--adjoint-intervals", type=int, default=0,
+                    help="dae workload: intervals of the adjoint cost measurement (0: none)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.workload != "plain" and args.impl == "ours":
-        print(json.dumps(run_batched(args) if args.workload == "batched" else run_adjoint(args)))
+        run = {"batched": run_batched, "adjoint": run_adjoint, "dae": run_dae}[args.workload]
+        print(json.dumps(run(args)))
         return
     if args.impl == "reference":
         if rank == 0:
