@@ -25,6 +25,31 @@
 
 namespace fo {
 
+// w[col[q]] -= lu[q] * z for q in [q0, q1): the factor entries of one row,
+// loaded eight at a time before their updates so that their latencies
+// overlap (the columns of one row are distinct, so the updates commute with
+// the loads).
+__device__ __forceinline__ void scatter_row(const double* __restrict__ lu, const int32_t* __restrict__ col, int q0,
+                                            int q1, double z, double* w, int L, int lane) {
+  constexpr int kBatch = 8;
+  int q = q0;
+  for (; q + kBatch <= q1; q += kBatch) {
+    double v[kBatch];
+    int c[kBatch];
+#pragma unroll
+    for (int i = 0; i < kBatch; ++i) {
+      v[i] = SCR(lu, q + i);
+      c[i] = __ldg(col + q + i);
+    }
+#pragma unroll
+    for (int i = 0; i < kBatch; ++i) WROW(c[i]) = fma(-v[i], z, WROW(c[i]));
+  }
+  for (; q < q1; ++q) {
+    const int c = __ldg(col + q);
+    WROW(c) = fma(-SCR(lu, q), z, WROW(c));
+  }
+}
+
 // Solve A^T x = b in place on w with the factors in lu (the diagonal slot
 // holds 1/pivot): U^T z = b by columns of U, then L^T x = z by rows of L.
 __device__ __noinline__ void lu_solve_transposed(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
@@ -37,18 +62,11 @@ __device__ __noinline__ void lu_solve_transposed(const SolveParams& p, const Lan
     const int dg = __ldg(diag + r), q1 = __ldg(rowp + r + 1);
     const double z = WROW(r) * SCR(lu, dg);
     WROW(r) = z;
-    for (int q = dg + 1; q < q1; ++q) {
-      const int c = __ldg(col + q);
-      WROW(c) = fma(-SCR(lu, q), z, WROW(c));
-    }
+    scatter_row(lu, col, dg + 1, q1, z, w, L, lane);
   }
   for (int r = n - 1; r >= 0; --r) {
     const double x = WROW(r);
-    const int dg = __ldg(diag + r);
-    for (int q = __ldg(rowp + r); q < dg; ++q) {
-      const int c = __ldg(col + q);
-      WROW(c) = fma(-SCR(lu, q), x, WROW(c));
-    }
+    scatter_row(lu, col, __ldg(rowp + r), __ldg(diag + r), x, w, L, lane);
   }
 }
 
