@@ -348,6 +348,8 @@ def run_batched(args):
         p = Part(wl.sm.mech, torch.from_numpy(wl.cells.Y0).to(dev), k.t(), wl.atol, wl.rtol, wl.dt,
                  photolysis=(photo, wl.sm.J[photo], wl.cells.phase))
         parts.append(p)
+    fma_rate = C.c_double()
+    _abi.check(lib.fo_fp64_fma_rate(C.byref(fma_rate)), "fo_fp64_fma_rate")
     mb = MultiBatch(parts)
     mb.capture()
     mb.run(args.warmup, graph=True)
@@ -361,6 +363,9 @@ def run_batched(args):
         torch.cuda.synchronize()
     s = e0.elapsed_time(e1) / 1e3
     total = sum(p.C for p in parts)
+    flops = sum(algorithmic_flops(p.plan, p.counts.cpu().numpy(), p.offsets.cpu().numpy()) for p in parts)
+    achieved = flops / s / 1e12
+    peak = 2.0 * fma_rate.value / 1e12
     per_part = []
     for wl, p in zip(wls, parts):
         c = p.counts.cpu().numpy()
@@ -374,7 +379,12 @@ def run_batched(args):
             "config": {"workload": "batched uneven: %d cells over 60/40, 120/260, 210/500, dt=60 s, half dark, "
                                    "one persistent launch per interval replayed as a CUDA graph" % total,
                        "slots": mb.slots},
-            "gpu_launches": args.steps * mb.launches_per_interval(), "parts": per_part, "clocks": clocks.summary()}
+            "gpu_launches": args.steps * mb.launches_per_interval(), "parts": per_part, "clocks": clocks.summary(),
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": DRAM_BYTES_PER_FLOP * flops / args.steps,
+                         "traffic_unit": "bytes per interval (the 210/500 ratio; smaller mechanisms stream less)",
+                         "time": "CUDA events around the graph replays of the timed intervals",
+                         "peak_source": "fo_fp64_fma_rate, same GPU, same run"}}
 
 
 def run_adjoint(args):

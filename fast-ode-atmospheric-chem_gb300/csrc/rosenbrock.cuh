@@ -50,11 +50,15 @@ struct Lane {
   bool active;   // this lane owns a real cell of the group
 };
 
-// Rates r_j = k_j * prod(x[react[j, :]]) (fastode/chem.py:86-87).
-__device__ void eval_rates(const SolveParams& p, const Lane& ln, const double* x, double* r) {
+// Rates r_j = k_j * prod(x[react[j, :]]) (fastode/chem.py:86-87). The
+// arrays are distinct scratch items, so the loads of several reactions can be
+// in flight together.
+__device__ void eval_rates(const SolveParams& p, const Lane& ln, const double* __restrict__ x,
+                           double* __restrict__ r) {
   const int L = ln.L, lane = ln.lane;
   const int n = p.t.n, R = p.t.R, P = p.t.P;
-  const double* kc = p.k + ln.cell * p.kcs;
+  const double* __restrict__ kc = p.k + ln.cell * p.kcs;
+#pragma unroll 4
   for (int j = 0; j < R; ++j) {
     double prod = 1.0;
     for (int q = 0; q < P; ++q) {
@@ -66,14 +70,24 @@ __device__ void eval_rates(const SolveParams& p, const Lane& ln, const double* x
 }
 
 // Forcing F = S r, species rows of the permuted stoichiometry
-// (fastode/chem.py:89-90).
-__device__ void eval_forcing(const SolveParams& p, const Lane& ln, const double* r, double* f) {
+// (fastode/chem.py:89-90). Each row's rates are loaded eight at a time
+// before they are summed in order, so their latencies overlap.
+__device__ void eval_forcing(const SolveParams& p, const Lane& ln, const double* __restrict__ r,
+                             double* __restrict__ f) {
+  constexpr int kBatch = 8;
   const int L = ln.L, lane = ln.lane;
   for (int i = 0; i < p.t.n; ++i) {
     double acc = 0.0;
     const int q1 = __ldg(p.t.s_ptr + i + 1);
-    for (int q = __ldg(p.t.s_ptr + i); q < q1; ++q)
-      acc = fma(__ldg(p.t.s_val + q), SCR(r, __ldg(p.t.s_rxn + q)), acc);
+    int q = __ldg(p.t.s_ptr + i);
+    for (; q + kBatch <= q1; q += kBatch) {
+      double v[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) v[b] = SCR(r, __ldg(p.t.s_rxn + q + b));
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) acc = fma(__ldg(p.t.s_val + q + b), v[b], acc);
+    }
+    for (; q < q1; ++q) acc = fma(__ldg(p.t.s_val + q), SCR(r, __ldg(p.t.s_rxn + q)), acc);
     SCR(f, i) = acc;
   }
 }
@@ -86,11 +100,13 @@ __device__ __noinline__ void eval_rhs(const SolveParams& p, const Lane& ln, cons
 // Negated Jacobian values in assembly order: d[j,p] = k_j prod_{q != p} x_q,
 // then -J = sum of (-S[i,j]) d[j,p] over the map's terms
 // (fastode/chem.py:92-102).
-__device__ __noinline__ void eval_negjac(const SolveParams& p, const Lane& ln, const double* x, double* d,
-                                         double* negj) {
+__device__ __noinline__ void eval_negjac(const SolveParams& p, const Lane& ln, const double* __restrict__ x,
+                                         double* __restrict__ d, double* __restrict__ negj) {
+  constexpr int kBatch = 8;
   const int L = ln.L, lane = ln.lane;
   const int n = p.t.n, R = p.t.R, P = p.t.P;
-  const double* kc = p.k + ln.cell * p.kcs;
+  const double* __restrict__ kc = p.k + ln.cell * p.kcs;
+#pragma unroll 4
   for (int j = 0; j < R; ++j) {
     const double kj = __ldg(kc + (int64_t)j * p.krs);
     for (int a = 0; a < P; ++a) {
@@ -106,8 +122,15 @@ __device__ __noinline__ void eval_negjac(const SolveParams& p, const Lane& ln, c
   for (int e = 0; e < p.t.nnzj; ++e) {
     double acc = 0.0;
     const int t1 = __ldg(p.t.jt_ptr + e + 1);
-    for (int t = __ldg(p.t.jt_ptr + e); t < t1; ++t)
-      acc = __dadd_rn(acc, __dmul_rn(__ldg(p.t.jt_val + t), SCR(d, __ldg(p.t.jt_idx + t))));
+    int t = __ldg(p.t.jt_ptr + e);
+    for (; t + kBatch <= t1; t += kBatch) {
+      double v[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) v[b] = SCR(d, __ldg(p.t.jt_idx + t + b));
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) acc = __dadd_rn(acc, __dmul_rn(__ldg(p.t.jt_val + t + b), v[b]));
+    }
+    for (; t < t1; ++t) acc = __dadd_rn(acc, __dmul_rn(__ldg(p.t.jt_val + t), SCR(d, __ldg(p.t.jt_idx + t))));
     SCR(negj, e) = acc;
   }
 }
