@@ -122,6 +122,25 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+# ---- replicas: one process per GPU, no data exchange -------------------------------------
+
+def max_over_ranks(seconds: float, world: int, device=None) -> float:
+    """The job's time with N replicas: the slowest rank's (an all-reduce MAX
+    over the process group; the identity on one process)."""
+    if world <= 1:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job throughput: every rank processes the same units (weak
+    scaling), divided by the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 # ---- the GPU arm ---------------------------------------------------------------------
 
 def algorithmic_flops(plan, counts_rows, offsets):
@@ -231,10 +250,7 @@ def run_ours(args, rank, world):
                                                     batch.counts.cpu().numpy().sum(0))) if n_plain == args.steps
                  else None}
         del pb
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(elapsed, world, dev)
     solve_ms = [a.elapsed_time(b) for a, b in ev]
     counts = batch.counts.cpu().numpy()
     statuses = batch.statuses()
@@ -242,7 +258,7 @@ def run_ours(args, rank, world):
     kernel_s = sum(solve_ms) / 1e3
     achieved = flops / kernel_s / 1e12
     peak = 2.0 * fma_rate.value / 1e12
-    value = Cc * args.steps * world / elapsed
+    value = job_value(Cc * args.steps, world, elapsed)
 
     # e2e through the public host API: host arrays in and out, copies timed
     e2e_steps = min(args.steps, args.e2e_steps)
@@ -342,10 +358,28 @@ def run_batched(args):
     lib = _abi.lib()
     sp = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
     wls = syn.batched_uneven(n_cells=args.cells, intervals=args.steps)
+    from fastode_gb300 import Algorithm
+    group_size, kernel, tuning = 32, "pipelined", None
+    if args.autotune:
+        # the group size and kernel of the launch, measured on 4,096 cells of
+        # the largest mechanism (one untimed and two timed intervals each)
+        from fastode_gb300.tune import autotune, candidates, measure_on_device
+        big = wls[-1].subset(slice(0, 4096))
+        measure = measure_on_device(big.sm.mech, big.cells.Y0, big.k_at, big.dt, big.atol, big.rtol)
+        from fastode_gb300.plan import plan_for
+        smem = plan_for(big.sm.mech).info["smem_doubles_per_cell"]
+        res = autotune(measure, smem, candidates(smem, group_sizes=(16, 32, 64), kernels=("pipelined", "plain"),
+                                                 persistent=(True,)))
+        group_size, kernel = res.best.group_size, res.best.kernel
+        tuning = {"sample": "4,096 cells of ros3-210x500, intervals 1-2 timed",
+                  "table": [{"kernel": c.kernel, "group_size": c.group_size,
+                             "cell_intervals_per_s": v} for c, v in res.table],
+                  "chosen": {"kernel": kernel, "group_size": group_size}}
     parts = []
     for wl in wls:
         k, photo = _device_rates(lib, wl.sm, wl.cells, dev, sp)
         p = Part(wl.sm.mech, torch.from_numpy(wl.cells.Y0).to(dev), k.t(), wl.atol, wl.rtol, wl.dt,
+                 group_size=group_size, algorithm=Algorithm(kernel=kernel),
                  photolysis=(photo, wl.sm.J[photo], wl.cells.phase))
         parts.append(p)
     fma_rate = C.c_double()
@@ -378,8 +412,9 @@ def run_batched(args):
             "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded generator)",
             "config": {"workload": "batched uneven: %d cells over 60/40, 120/260, 210/500, dt=60 s, half dark, "
                                    "one persistent launch per interval replayed as a CUDA graph" % total,
-                       "slots": mb.slots},
+                       "slots": mb.slots, "group_size": group_size, "kernel": kernel},
             "gpu_launches": args.steps * mb.launches_per_interval(), "parts": per_part, "clocks": clocks.summary(),
+            "autotune": tuning,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": DRAM_BYTES_PER_FLOP * flops / args.steps,
                          "traffic_unit": "bytes per interval (the 210/500 ratio; smaller mechanisms stream less)",
@@ -584,6 +619,8 @@ def main():
                     help="plain: the 210/500 drop-in workload (default, the headline line); batched: the "
                          "three-mechanism persistent launch; adjoint: forward+adjoint cost; dae: the RODAS3 "
                          "constrained workload with its adjoint cost")
+    ap.add_argument("--autotune", action="store_true",
+                    help="batched workload: choose group size and kernel with the autotuner on a sample")
     ap.add_argument("--fd-directions", type=int, default=2,
                     help="central-difference directions checking the adjoint gradient")
     ap.add_argument("--adjoint-intervals", type=int, default=0,
