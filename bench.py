@@ -367,9 +367,10 @@ def run_batched(args):
         big = wls[-1].subset(slice(0, 4096))
         measure = measure_on_device(big.sm.mech, big.cells.Y0, big.k_at, big.dt, big.atol, big.rtol)
         from fastode_gb300.plan import plan_for
-        smem = plan_for(big.sm.mech).info["smem_doubles_per_cell"]
-        res = autotune(measure, smem, candidates(smem, group_sizes=(16, 32, 64), kernels=("pipelined", "plain"),
-                                                 persistent=(True,)))
+        bp = plan_for(big.sm.mech)
+        smem = {k: bp.smem_items(k) for k in ("pipelined", "plain", "compact")}
+        res = autotune(measure, smem, candidates(smem, group_sizes=(16, 32, 64),
+                                                 kernels=("compact", "pipelined", "plain"), persistent=(True,)))
         group_size, kernel = res.best.group_size, res.best.kernel
         tuning = {"sample": "4,096 cells of ros3-210x500, intervals 1-2 timed",
                   "table": [{"kernel": c.kernel, "group_size": c.group_size,
@@ -608,7 +609,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--cells", type=int, default=65536)
     ap.add_argument("--slots", type=int, default=0)
-    ap.add_argument("--kernel", default="pipelined", choices=["pipelined", "plain"])
+    ap.add_argument("--kernel", default="pipelined", choices=["pipelined", "plain", "compact"])
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=12)

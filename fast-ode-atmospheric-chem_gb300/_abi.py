@@ -36,7 +36,7 @@ class PlanInfo(C.Structure):
                 ("ordering", C.c_int32), ("nnz_lu", C.c_int32), ("nnz_l", C.c_int32), ("nnz_u", C.c_int32),
                 ("lu_fma", C.c_int64), ("solve_fma", C.c_int64), ("jac_terms", C.c_int32),
                 ("stoich_nnz", C.c_int32), ("scratch_doubles_per_cell", C.c_int64),
-                ("smem_doubles_per_cell", C.c_int32)]
+                ("smem_doubles_per_cell", C.c_int32), ("compact_smem_doubles_per_cell", C.c_int32)]
 
     def as_dict(self):
         d = {name: getattr(self, name) for name, _ in self._fields_}
@@ -54,7 +54,7 @@ class Options(C.Structure):
                 ("reductions", C.c_double * 8), ("small", C.c_double)]
 
 
-VARIANTS = {"pipelined": 0, "plain": 1}
+VARIANTS = {"pipelined": 0, "plain": 1, "compact": 2}
 LOOPS = {"algorithm": 0, "restarting": 1, "backward-euler": 2}
 SCORE_RULES = {"ts1": 0, "digits": 1}
 

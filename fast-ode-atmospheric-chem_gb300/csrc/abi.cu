@@ -102,8 +102,18 @@ int region_items(const fo::HostTables& t) {
   return t.n > t.max_row_len + ring ? t.n : t.max_row_len + ring;
 }
 
-size_t smem_bytes(const fo::HostTables& t, int lanes) {
-  return sizeof(double) * (32 + (size_t)region_items(t) * lanes);
+// The compact variant's items per lane: half a row and its ring, or half the
+// solve vector.
+int compact_region_items(const fo::HostTables& t) {
+  if (t.ce_ptr.empty()) return region_items(t);
+  const int rows = t.cmax_half + fo::kCompactRing * fo::kStreamChunk;
+  const int half = std::max(t.csm, t.n - t.csm);
+  return std::max(rows, half);
+}
+
+size_t smem_bytes(const fo::HostTables& t, int lanes, int variant = FO_VARIANT_PIPELINED) {
+  const int items = variant == FO_VARIANT_COMPACT ? compact_region_items(t) : region_items(t);
+  return sizeof(double) * (32 + (size_t)items * lanes);
 }
 
 constexpr size_t kHeader = 256;  // queue counter at the start of the workspace
@@ -133,6 +143,7 @@ void fill_info(const fo::HostTables& t, fo_plan_info* info) {
   info->stoich_nnz = (int32_t)t.s_rxn.size();
   info->scratch_doubles_per_cell = layout_of(t).items;
   info->smem_doubles_per_cell = region_items(t);
+  info->compact_smem_doubles_per_cell = compact_region_items(t);
 }
 
 fo::SolveParams base_params(const fo_plan* plan) {
@@ -187,7 +198,10 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
          o_lur = append(buf, t.lu_row_ptr), o_lud = append(buf, t.lu_diag), o_luc = append(buf, t.lu_col),
          o_elp = append(buf, t.el_ptr), o_el = append(buf, t.el), o_sf = append(buf, t.sf),
          o_sb = append(buf, t.sb), o_jpos = append(buf, t.j_lu_pos), o_elpk = append(buf, t.elp),
-         o_stp = append(buf, t.st_ptr), o_sts = append(buf, t.st_sp), o_stv = append(buf, t.st_val);
+         o_stp = append(buf, t.st_ptr), o_sts = append(buf, t.st_sp), o_stv = append(buf, t.st_val),
+         o_css = append(buf, t.cs_split), o_csj = append(buf, t.cs_jsplit), o_cep_ptr = append(buf, t.ce_ptr),
+         o_cep = append(buf, t.cep), o_cfa = append(buf, t.csf_a), o_cfb = append(buf, t.csf_b),
+         o_cbb = append(buf, t.csb_b), o_cba = append(buf, t.csb_a);
   cudaError_t e = cudaGetDevice(&plan->device);
   if (e != cudaSuccess) {
     delete plan;
@@ -237,6 +251,20 @@ int fo_plan_create(const fo_mechanism_desc* mech, int32_t ordering, fo_plan** ou
   d.nsf = (int)(t.sf.size() / 2);
   d.nsb = (int)(t.sb.size() / 2);
   d.j_pos = reinterpret_cast<const int32_t*>(b + o_jpos);
+  d.cs_split = reinterpret_cast<const int32_t*>(b + o_css);
+  d.cs_jsplit = reinterpret_cast<const int32_t*>(b + o_csj);
+  d.ce_ptr = reinterpret_cast<const int32_t*>(b + o_cep_ptr);
+  d.cep = t.ce_ptr.empty() ? nullptr : reinterpret_cast<const uint32_t*>(b + o_cep);
+  d.cmax_half = t.cmax_half;
+  d.csm = t.csm;
+  d.csf_a = reinterpret_cast<const int2*>(b + o_cfa);
+  d.csf_b = reinterpret_cast<const int2*>(b + o_cfb);
+  d.csb_b = reinterpret_cast<const int2*>(b + o_cbb);
+  d.csb_a = reinterpret_cast<const int2*>(b + o_cba);
+  d.ncsf_a = (int)(t.csf_a.size() / 2);
+  d.ncsf_b = (int)(t.csf_b.size() / 2);
+  d.ncsb_b = (int)(t.csb_b.size() / 2);
+  d.ncsb_a = (int)(t.csb_a.size() / 2);
   d.max_row_len = t.max_row_len;
   d.region = region_items(t);
   d.has_constraints = 0;
@@ -286,14 +314,17 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
     return fail(FO_E_INVALID, "null argument");
   if (opt->tableau != FO_TABLEAU_ROS3 && opt->tableau != FO_TABLEAU_RODAS3)
     return fail(FO_E_INVALID, "unknown tableau");
-  if (opt->variant != FO_VARIANT_PIPELINED && opt->variant != FO_VARIANT_PLAIN)
+  if (opt->variant != FO_VARIANT_PIPELINED && opt->variant != FO_VARIANT_PLAIN && opt->variant != FO_VARIANT_COMPACT)
     return fail(FO_E_INVALID, "unknown kernel variant");
+  int variant = opt->variant;
+  if (variant == FO_VARIANT_COMPACT && plan->dev.cep == nullptr) variant = FO_VARIANT_PIPELINED;
+  if (variant == FO_VARIANT_PIPELINED && plan->dev.elp == nullptr) variant = FO_VARIANT_PLAIN;
   if (max_group_cells <= 0 || max_group_cells > kMaxLanes)
     return fail(FO_E_UNSUPPORTED, "group size must be 1..256 cells");
   if (!(dt > 0.0)) return fail(FO_E_INVALID, "dt must be positive");
   if (opt->max_steps < 0) return fail(FO_E_INVALID, "max_steps must be non-negative");
   const int lanes = lanes_for(max_group_cells);
-  const size_t smem = smem_bytes(plan->host, lanes);
+  const size_t smem = smem_bytes(plan->host, lanes, variant);
   int dev = 0, smem_max = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
@@ -312,7 +343,7 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
   p.o.quantize = opt->quantize;
   p.o.carry_memory = opt->carry_memory;
   p.o.max_steps = opt->max_steps;
-  p.o.variant = opt->variant;
+  p.o.variant = variant;
   if (opt->loop != FO_LOOP_ALGORITHM && opt->loop != FO_LOOP_RESTARTING && opt->loop != FO_LOOP_BACKWARD_EULER)
     return fail(FO_E_INVALID, "unknown loop");
   p.o.loop = opt->loop;
@@ -330,7 +361,6 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
   }
   // the pipelined kernel needs the packed stream (positions below 65,536 and
   // rows shorter than 32,767 entries); larger mechanisms run the plain loops
-  if (p.o.variant == FO_VARIANT_PIPELINED && plan->dev.elp == nullptr) p.o.variant = FO_VARIANT_PLAIN;
   p.o.k_exp = 3.0;  // embedded order 2 for both tableaus
   p.ngroups = ngroups;
   p.group_offsets = group_offsets;
@@ -463,7 +493,7 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
                      d.y_species_stride, d.k, d.k_cell_stride, d.k_reaction_stride, d.atol, d.rtol, d.dt, d.memory,
                      d.counts, d.status, &params[j], &sm);
     if (rc != FO_OK) return rc;
-    smem = std::max(smem, sizeof(double) * (32 + (size_t)region_items(d.plan->host) * L.lanes));
+    smem = std::max(smem, smem_bytes(d.plan->host, L.lanes, params[j].o.variant));
     starts[j + 1] = starts[j] + d.ngroups;
   }
   int dev = 0, smem_max = 0;
@@ -572,6 +602,10 @@ int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngro
   fo_adjoint_workspace_bytes(plan, ngroups, max_group_cells, max_steps, &need);
   if (workspace_bytes < need) return fail(FO_E_WORKSPACE, "workspace too small");
   a.al = adjoint_layout(plan->host, max_steps);
+  if (a.p.o.variant == FO_VARIANT_COMPACT) {     // the transposed solves need the whole vector on chip
+    a.p.o.variant = plan->dev.elp ? FO_VARIANT_PIPELINED : FO_VARIANT_PLAIN;
+    smem = smem_bytes(plan->host, a.p.lanes, a.p.o.variant);
+  }
   a.p.slot_doubles = a.al.items * a.p.lanes;
   a.p.scratch = reinterpret_cast<double*>(static_cast<char*>(workspace) + kHeader);
   a.Ycp = Y;

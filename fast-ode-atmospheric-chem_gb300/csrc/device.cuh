@@ -35,6 +35,18 @@ struct DevTables {
   const int2* sb;             // backward-solve stream
   int nsf, nsb;               // entries of each solve stream
   const int32_t* j_pos;       // nnzj: position of each Jacobian entry in the LU storage
+  // the compact variant (null cep when the tables do not fit)
+  const int32_t* cs_split;    // n: first slot of each row's second pass
+  const int32_t* cs_jsplit;   // n: first Jacobian entry of each row's second pass
+  const int32_t* ce_ptr;      // 2n+1: the passes' entries
+  const uint32_t* cep;        // the passes' entries, packed
+  int cmax_half;              // slots of the largest pass
+  int csm;                    // rows of the solve vector's first half
+  const int2* csf_a;          // the split solves' streams
+  const int2* csf_b;
+  const int2* csb_b;
+  const int2* csb_a;
+  int ncsf_a, ncsf_b, ncsb_b, ncsb_a;
   int max_row_len;            // longest row of the filled pattern
   int region;                 // shared-memory items per lane (work row / ring / solve vector)
   int has_constraints;

@@ -331,12 +331,102 @@ __device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln,
   }
 }
 
+// ---- the compact factorization (FO_VARIANT_COMPACT) ------------------------------
+//
+// Row r is eliminated in two passes over halves of its slots (symbolic.h):
+// pass A is the elimination restricted to the row's leading columns and
+// stores its multipliers as it makes them; pass B applies every multiplier's
+// updates of the trailing columns, in the same order, reloading A's
+// multipliers from the LU storage with an ordinary load (this thread stored
+// them; an asynchronous copy would not be ordered after that store). The
+// work row therefore holds half a row, and the factors are the pipelined
+// ones bit for bit. The U operands are staged one chunk ahead in a two-slot
+// ring: with twice as many groups resident per SM, a deeper ring buys nothing.
+
+__device__ __noinline__ void factor_compact(const SolveParams& p, const Lane& ln, double alpha, const double* negj,
+                                            double* lu, double* w, bool alg_only) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n;
+  const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
+  const int32_t* __restrict__ diag = p.t.lu_diag;
+  double* ring = w + (int64_t)p.t.cmax_half * L;
+  for (int r = 0; r < n; ++r) {
+    const int q0 = __ldg(rowp + r), len = __ldg(rowp + r + 1) - q0, dslot = __ldg(diag + r) - q0;
+    const int split = __ldg(p.t.cs_split + r), jsplit = __ldg(p.t.cs_jsplit + r);
+    const double mr = __ldg(p.t.mass + r);
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+      const int base = pass ? split : 0, cnt = pass ? len - split : split;
+      for (int s = 0; s < cnt; ++s) WROW(s) = 0.0;
+      if (!alg_only || mr == 0.0) {
+        const int e0 = pass ? jsplit : __ldg(p.t.j_row_ptr + r);
+        const int e1 = pass ? __ldg(p.t.j_row_ptr + r + 1) : jsplit;
+        for (int e = e0; e < e1; ++e) WROW(__ldg(p.t.j_pos + e) - q0 - base) = SCR(negj, e);
+      }
+      const bool has_diag = dslot >= base && dslot < base + cnt;
+      if (has_diag) WROW(dslot - base) = __dadd_rn(WROW(dslot - base), __dmul_rn(alpha, mr));
+      const int t0 = __ldg(p.t.ce_ptr + 2 * r + pass);
+      const int nch = (__ldg(p.t.ce_ptr + 2 * r + pass + 1) - t0) / kChunk;
+      const uint32_t* meta = p.t.cep + t0;
+      double* qlu = lu + (int64_t)(q0 + base) * L;     // this pass's slot s stands for lu[q0 + base + s]
+      double l = 0.0;
+      Meta mc, mi;
+      if (nch > 0) {
+        meta_load(meta, mc);
+        ring_issue(mc, lu, L, lane, ring);
+      }
+      ring_commit();
+      if (nch > 1) meta_load(meta + kChunk, mi);
+#pragma unroll 1
+      for (int c = 0; c < nch; ++c) {
+        Meta mn;
+        if (c + 2 < nch) meta_load(meta + (c + 2) * kChunk, mn);
+        if (c + 1 < nch) ring_issue(mi, lu, L, lane, ring + (int64_t)((c + 1) % kCompactRing) * kChunk * L);
+        ring_commit();
+        asm volatile("cp.async.wait_group %0;" ::"n"(kCompactRing - 1) : "memory");
+        const double* rs = ring + (int64_t)(c % kCompactRing) * kChunk * L;
+        double wv[kChunk];
+#pragma unroll
+        for (int s = 0; s < kChunk; ++s) {
+          const uint32_t y = meta_at(mc, s) & 0x7fffu;
+          wv[s] = y < kReloadSlot ? WROW(y) : 0.0;
+        }
+#pragma unroll
+        for (int s = 0; s < kChunk; ++s) {
+          const uint32_t word = meta_at(mc, s);
+          const uint32_t y = word & 0x7fffu;
+          if (word & 0x8000u) {
+            l = wv[s] * rs[s * L + lane];
+            SCR(qlu, y) = l;
+          } else if (y == kReloadSlot) {
+            l = lu[(int64_t)(word >> 16) * L + lane];
+          } else if (y != 0x7fffu) {
+            wv[s] = fma(-l, rs[s * L + lane], wv[s]);
+          }
+        }
+#pragma unroll
+        for (int s = 0; s < kChunk; ++s) {
+          const uint32_t word = meta_at(mc, s);
+          const uint32_t y = word & 0x7fffu;
+          if (!(word & 0x8000u) && y < kReloadSlot) WROW(y) = wv[s];
+        }
+        mc = mi;
+        mi = mn;
+      }
+      if (has_diag) WROW(dslot - base) = 1.0 / WROW(dslot - base);
+      for (int s = dslot > base ? dslot - base : 0; s < cnt; ++s) SCR(qlu, s) = WROW(s);
+    }
+  }
+}
+
 // Forward and backward substitution driven by the solve streams
 // (symbolic.h): the factor entries are loaded one chunk ahead of their use
 // (they do not depend on the solution), the solution entries are read from
 // shared memory when the chunk computes.
-__device__ __forceinline__ void solve_load(const int2* __restrict__ meta, const double* __restrict__ lu, int L,
-                                           int lane, int4 (&m)[kChunk / 2], double (&v)[kChunk]) {
+template <bool kMixed>
+__device__ __forceinline__ void solve_load(const int2* __restrict__ meta, const double* __restrict__ lu,
+                                           const double* xg, int L, int lane, int4 (&m)[kChunk / 2],
+                                           double (&v)[kChunk], double (&g)[kChunk]) {
 #pragma unroll
   for (int s = 0; s < kChunk / 2; ++s) m[s] = __ldg(reinterpret_cast<const int4*>(meta) + s);
 #pragma unroll
@@ -345,16 +435,24 @@ __device__ __forceinline__ void solve_load(const int2* __restrict__ meta, const 
     const int p1 = m[s].z >= 0 ? m[s].z : -1 - m[s].z;
     v[2 * s] = lu[(int64_t)p0 * L + lane];
     v[2 * s + 1] = lu[(int64_t)p1 * L + lane];
+    if (kMixed) {
+      // an operand of the other, finished half of the vector (global memory)
+      const int y0 = m[s].y, y1 = m[s].w;
+      g[2 * s] = (y0 >= 0 && (y0 & kGlobalOperand)) ? xg[(int64_t)(y0 & ~kGlobalOperand) * L + lane] : 0.0;
+      g[2 * s + 1] = (y1 >= 0 && (y1 & kGlobalOperand)) ? xg[(int64_t)(y1 & ~kGlobalOperand) * L + lane] : 0.0;
+    }
   }
 }
 
 // Four partial sums per row, entry s of a chunk feeding sum s mod 4: the
 // row's FMAs form four independent chains instead of one, so FP64 latency
 // overlaps.
-template <bool kBackward>
-__device__ __forceinline__ void solve_entry(int s, int y, double v, double* w, int L, int lane, double (&acc)[4]) {
+template <bool kBackward, bool kMixed>
+__device__ __forceinline__ void solve_entry(int s, int y, double v, double gv, double* w, int L, int lane,
+                                            double (&acc)[4]) {
   if (y >= 0) {
-    acc[s & 3] = fma(-v, WROW(y), acc[s & 3]);
+    const double x = (kMixed && (y & kGlobalOperand)) ? gv : WROW(y);
+    acc[s & 3] = fma(-v, x, acc[s & 3]);
   } else if (y != kNoop) {
     const int r = -1 - y;
     const double b = WROW(r) + ((acc[0] + acc[1]) + (acc[2] + acc[3]));
@@ -363,36 +461,61 @@ __device__ __forceinline__ void solve_entry(int s, int y, double v, double* w, i
   }
 }
 
-template <bool kBackward>
-__device__ __forceinline__ void solve_compute(const int4 (&m)[kChunk / 2], const double (&v)[kChunk], double* w,
-                                              int L, int lane, double (&acc)[4]) {
+template <bool kBackward, bool kMixed>
+__device__ __forceinline__ void solve_compute(const int4 (&m)[kChunk / 2], const double (&v)[kChunk],
+                                              const double (&g)[kChunk], double* w, int L, int lane, double (&acc)[4]) {
 #pragma unroll
   for (int s = 0; s < kChunk / 2; ++s) {
-    solve_entry<kBackward>(2 * s, m[s].y, v[2 * s], w, L, lane, acc);
-    solve_entry<kBackward>(2 * s + 1, m[s].w, v[2 * s + 1], w, L, lane, acc);
+    solve_entry<kBackward, kMixed>(2 * s, m[s].y, v[2 * s], g[2 * s], w, L, lane, acc);
+    solve_entry<kBackward, kMixed>(2 * s + 1, m[s].w, v[2 * s + 1], g[2 * s + 1], w, L, lane, acc);
   }
 }
 
-template <bool kBackward>
-__device__ void solve_stream(const int2* __restrict__ st, int nst, const double* lu, double* w, int L, int lane) {
+// kMixed: the stream's operands may lie in xg (kGlobalOperand set).
+template <bool kBackward, bool kMixed = false>
+__device__ void solve_stream(const int2* __restrict__ st, int nst, const double* lu, double* w, int L, int lane,
+                             const double* xg = nullptr) {
   int4 mA[kChunk / 2], mB[kChunk / 2];
-  double vA[kChunk], vB[kChunk];
+  double vA[kChunk], vB[kChunk], gA[kChunk], gB[kChunk];
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   const int nch = nst / kChunk;
-  solve_load(st, lu, L, lane, mA, vA);
+  if (nch == 0) return;            // an empty half (a one-species system)
+  solve_load<kMixed>(st, lu, xg, L, lane, mA, vA, gA);
 #pragma unroll 1
   for (int c = 0; c < nch; c += 2) {
-    if (c + 1 < nch) solve_load(st + (c + 1) * kChunk, lu, L, lane, mB, vB);
-    solve_compute<kBackward>(mA, vA, w, L, lane, acc);
+    if (c + 1 < nch) solve_load<kMixed>(st + (c + 1) * kChunk, lu, xg, L, lane, mB, vB, gB);
+    solve_compute<kBackward, kMixed>(mA, vA, gA, w, L, lane, acc);
     if (c + 1 >= nch) break;
-    if (c + 2 < nch) solve_load(st + (c + 2) * kChunk, lu, L, lane, mA, vA);
-    solve_compute<kBackward>(mB, vB, w, L, lane, acc);
+    if (c + 2 < nch) solve_load<kMixed>(st + (c + 2) * kChunk, lu, xg, L, lane, mA, vA, gA);
+    solve_compute<kBackward, kMixed>(mB, vB, gB, w, L, lane, acc);
   }
 }
 
 __device__ __noinline__ void lu_solve_pipelined(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
   solve_stream<false>(p.t.sf, p.t.nsf, lu, w, ln.L, ln.lane);
   solve_stream<true>(p.t.sb, p.t.nsb, lu, w, ln.L, ln.lane);
+}
+
+// The compact solves: b and x are per-lane vectors in global memory (they may
+// alias) and shared memory holds one half of the vector at a time. Forward
+// over rows [0, csm) needs only that half; the finished half is stored, and
+// forward over rows [csm, n) then reads it from x, as does nothing else until
+// backward over rows [n-1, csm) has finished the second half, which is stored
+// for backward over rows [csm-1, 0) to read.
+__device__ __noinline__ void lu_solve_compact(const SolveParams& p, const Lane& ln, const double* lu, double* w,
+                                              const double* b, double* x) {
+  const int L = ln.L, lane = ln.lane;
+  const int n = p.t.n, m = p.t.csm;
+  for (int i = 0; i < m; ++i) WROW(i) = SCR(b, i);
+  solve_stream<false>(p.t.csf_a, p.t.ncsf_a, lu, w, L, lane);
+  for (int i = 0; i < m; ++i) SCR(x, i) = WROW(i);
+  for (int i = m; i < n; ++i) WROW(i - m) = SCR(b, i);
+  solve_stream<false, true>(p.t.csf_b, p.t.ncsf_b, lu, w, L, lane, x);
+  solve_stream<true>(p.t.csb_b, p.t.ncsb_b, lu, w, L, lane);
+  for (int i = m; i < n; ++i) SCR(x, i) = WROW(i - m);
+  for (int i = 0; i < m; ++i) WROW(i) = SCR(x, i);
+  solve_stream<true, true>(p.t.csb_a, p.t.ncsb_a, lu, w, L, lane, x);
+  for (int i = 0; i < m; ++i) SCR(x, i) = WROW(i);
 }
 
 // Forward and backward substitution in place on w (fastode/linalg.py:80-81).
@@ -419,6 +542,7 @@ __device__ void lu_solve(const SolveParams& p, const Lane& ln, const double* lu,
 __device__ void factor_any(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
                            double* w, bool alg_only) {
   if (p.o.variant == FO_VARIANT_PLAIN) factor(p, ln, alpha, negj, lu, w, alg_only);
+  else if (p.o.variant == FO_VARIANT_COMPACT) factor_compact(p, ln, alpha, negj, lu, w, alg_only);
   else factor_stream(p, ln, alpha, negj, lu, w, alg_only);
 }
 
@@ -430,6 +554,10 @@ __device__ __forceinline__ void solve_in_w(const SolveParams& p, const Lane& ln,
 // x = A^-1 b with the factors in lu (b and x per-lane vectors, may alias).
 __device__ void solve_into(const SolveParams& p, const Lane& ln, const double* lu, double* w, const double* b,
                            double* x) {
+  if (p.o.variant == FO_VARIANT_COMPACT) {
+    lu_solve_compact(p, ln, lu, w, b, x);
+    return;
+  }
   const int L = ln.L, lane = ln.lane;
   for (int i = 0; i < p.t.n; ++i) WROW(i) = SCR(b, i);
   solve_in_w(p, ln, lu, w);
@@ -479,6 +607,8 @@ __device__ __noinline__ double attempt(const SolveParams& p, const Lane& ln, dou
       ++c_rhs;
       forcing = Ft;
     }
+    double* Kr = K + (int64_t)r * n * L;
+    const bool compact = p.o.variant == FO_VARIANT_COMPACT;   // right-hand side in Kr, solved in place
     for (int i = 0; i < n; ++i) {
       double v = SCR(forcing, i);
       for (int s = 0; s < r; ++s) {
@@ -489,11 +619,15 @@ __device__ __noinline__ double attempt(const SolveParams& p, const Lane& ln, dou
           v = __dadd_rn(v, __dmul_rn(coef, ks));
         }
       }
-      WROW(i) = v;
+      if (compact) SCR(Kr, i) = v;
+      else WROW(i) = v;
     }
-    solve_in_w(p, ln, lu, w);
-    double* Kr = K + (int64_t)r * n * L;
-    for (int i = 0; i < n; ++i) SCR(Kr, i) = WROW(i);
+    if (compact) {
+      lu_solve_compact(p, ln, lu, w, Kr, Kr);
+    } else {
+      solve_in_w(p, ln, lu, w);
+      for (int i = 0; i < n; ++i) SCR(Kr, i) = WROW(i);
+    }
     ++c_solves;
   }
   // Y_new, E and the weighted sum of squares
@@ -833,6 +967,7 @@ __device__ __noinline__ void solve_group_backward_euler(const SolveParams& p, in
   double* dd = scr + p.sl.d * L;
   double* rr = scr + p.sl.r * L;
   double* lu = scr + p.sl.lu * L;
+  const bool compact = p.o.variant == FO_VARIANT_COMPACT;   // Newton update solved in place in F
   for (int i = 0; i < n; ++i) {
     const double v = p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss];
     SCR(Yn, i) = v;
@@ -856,14 +991,18 @@ __device__ __noinline__ void solve_group_backward_euler(const SolveParams& p, in
       ++c_jac;
       factor_any(p, ln, 1.0 / H, negj, lu, w, false);
       ++c_lu;
-      for (int i = 0; i < n; ++i)
-        WROW(i) = __dsub_rn(SCR(F, i), __ddiv_rn(__dsub_rn(SCR(Yn1, i), SCR(Yn, i)), H));
-      solve_in_w(p, ln, lu, w);
+      for (int i = 0; i < n; ++i) {
+        const double v = __dsub_rn(SCR(F, i), __ddiv_rn(__dsub_rn(SCR(Yn1, i), SCR(Yn, i)), H));
+        if (compact) SCR(F, i) = v;
+        else WROW(i) = v;
+      }
+      if (compact) lu_solve_compact(p, ln, lu, w, F, F);
+      else solve_in_w(p, ln, lu, w);
       ++c_solves;
       ++iterations;
       bool conv = true;
       for (int i = 0; i < n; ++i) {
-        const double d = WROW(i);
+        const double d = compact ? SCR(F, i) : WROW(i);
         const double y = clamp0(__dadd_rn(SCR(Yn1, i), d));
         SCR(Yn1, i) = y;
         if (iterations > 1) {

@@ -197,6 +197,108 @@ int64_t cost_of(const fo_mechanism_desc& m, const std::vector<int>& order) {
 
 }  // namespace
 
+// The compact variant's tables (see HostTables), built from the LU structure
+// and the Jacobian's positions in it.
+void build_compact(HostTables* t) {
+  const int n = t->n;
+  t->cs_split.assign(n, 0);
+  t->cs_jsplit.assign(n, 0);
+  t->ce_ptr.assign(1, 0);
+  t->cep.clear();
+  t->cmax_half = 0;
+  if ((int64_t)t->lu_col.size() > 65536 || t->max_row_len >= 0x7ffe) {
+    t->ce_ptr.clear();
+    return;
+  }
+  std::vector<int> slot_of(n, -1);
+  std::vector<int64_t> touched(n, -1);
+  auto entries = [&]() { return (int64_t)t->cep.size(); };
+  auto pad = [&]() {
+    while (entries() % kStreamChunk != 0) t->cep.push_back(0x7fffu);
+  };
+  auto pad_chunk = [&]() {
+    t->cep.push_back(0x7fffu);
+    pad();
+  };
+  // an entry that touches `slot` (relative to the pass) may not share a chunk
+  // with an earlier update of it
+  auto place = [&](int slot) {
+    while (touched[slot] >= entries() / kStreamChunk) pad_chunk();
+  };
+  for (int r = 0; r < n; ++r) {
+    const int q0 = t->lu_row_ptr[r], len = t->lu_row_ptr[r + 1] - q0, dg = t->lu_diag[r];
+    const int split = (len + 1) / 2;
+    t->cs_split[r] = split;
+    t->cmax_half = std::max(t->cmax_half, std::max(split, len - split));
+    for (int q = q0; q < q0 + len; ++q) slot_of[t->lu_col[q]] = q - q0;
+    for (int pass = 0; pass < 2; ++pass) {
+      const int base = pass ? split : 0, cnt = pass ? len - split : split;
+      for (int s = 0; s < cnt; ++s) touched[s] = -2;
+      for (int q = q0; q < dg; ++q) {
+        const int k = t->lu_col[q], ks = q - q0;
+        const bool in_a = ks < split;
+        if (pass == 0 && !in_a) break;                       // pass A: the leading multipliers only
+        bool opened = false;
+        if (pass == 0 || !in_a) {                            // the pass that makes l_rk
+          place(ks - base);
+          t->cep.push_back(((uint32_t)t->lu_diag[k] << 16) | 0x8000u | (uint32_t)(ks - base));
+          opened = true;
+        }
+        for (int u = t->lu_diag[k] + 1; u < t->lu_row_ptr[k + 1]; ++u) {
+          const int y = slot_of[t->lu_col[u]];
+          if ((y >= split) != (pass == 1)) continue;         // the other pass's column
+          if (!opened) {                                     // pass B reloads a multiplier of pass A
+            t->cep.push_back(((uint32_t)q << 16) | kReloadSlot);
+            opened = true;
+          }
+          place(y - base);
+          touched[y - base] = entries() / kStreamChunk;
+          t->cep.push_back(((uint32_t)u << 16) | (uint32_t)(y - base));
+        }
+      }
+      pad();
+      t->ce_ptr.push_back((int32_t)t->cep.size());
+    }
+    int e = t->j_row_ptr[r];
+    while (e < t->j_row_ptr[r + 1] && t->j_lu_pos[e] - q0 < split) ++e;
+    t->cs_jsplit[r] = e;
+  }
+  // the split solves
+  const int m = (n + 1) / 2;
+  t->csm = m;
+  auto finish = [](std::vector<int32_t>* st) {
+    while ((st->size() / 2) % kStreamChunk != 0) {
+      st->push_back(-1);
+      st->push_back(kNoop);
+    }
+  };
+  auto operand = [&](int col, int half_base, int half_end) {
+    return (col >= half_base && col < half_end) ? col - half_base : (col | kGlobalOperand);
+  };
+  for (std::vector<int32_t>* st : {&t->csf_a, &t->csf_b, &t->csb_b, &t->csb_a}) st->clear();
+  for (int r = 0; r < n; ++r) {                            // forward: L y = b
+    std::vector<int32_t>* st = r < m ? &t->csf_a : &t->csf_b;
+    const int hb = r < m ? 0 : m, he = r < m ? m : n;
+    for (int q = t->lu_row_ptr[r]; q < t->lu_diag[r]; ++q) {
+      st->push_back(q);
+      st->push_back(operand(t->lu_col[q], hb, he));
+    }
+    st->push_back(-1);
+    st->push_back(-1 - (r - hb));
+  }
+  for (int r = n - 1; r >= 0; --r) {                       // backward: U x = y
+    std::vector<int32_t>* st = r >= m ? &t->csb_b : &t->csb_a;
+    const int hb = r < m ? 0 : m, he = r < m ? m : n;
+    for (int q = t->lu_diag[r] + 1; q < t->lu_row_ptr[r + 1]; ++q) {
+      st->push_back(q);
+      st->push_back(operand(t->lu_col[q], hb, he));
+    }
+    st->push_back(-1 - t->lu_diag[r]);
+    st->push_back(-1 - (r - hb));
+  }
+  for (std::vector<int32_t>* st : {&t->csf_a, &t->csf_b, &t->csb_b, &t->csb_a}) finish(st);
+}
+
 std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t) {
   std::string err = validate(m);
   if (!err.empty()) return err;
@@ -413,6 +515,7 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
     }
     t->j_row_ptr.push_back((int32_t)t->j_col.size());
   }
+  build_compact(t);
   return "";
 }
 

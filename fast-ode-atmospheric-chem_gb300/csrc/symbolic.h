@@ -58,6 +58,30 @@ struct HostTables {
   // position or a slot does not fit (the plain kernel then runs instead).
   std::vector<uint32_t> elp;
 
+  // Compact factorization and solves (FO_VARIANT_COMPACT), which keep half a
+  // row and half the solve vector in shared memory. Row r is eliminated in two
+  // passes over its slots, A = [0, cs_split[r]) and B = [cs_split[r], len):
+  // A is the elimination restricted to the row's leading columns (its
+  // multipliers are stored in the LU storage as they are made); B applies
+  // every multiplier's updates of the trailing columns in the same order,
+  // reloading the multipliers A made, and makes the rest. ce_ptr[2r + pass]
+  // delimits the pass's entries in cep, packed as elp with slots relative to
+  // the pass and kReloadSlot marking a reload (l = lu[position]); padded to
+  // whole chunks. cs_jsplit[r] is the first Jacobian entry (assembly order)
+  // of pass B. Empty when a slot or a position does not fit.
+  std::vector<int32_t> cs_split, cs_jsplit, ce_ptr;
+  std::vector<uint32_t> cep;
+  int cmax_half = 0;
+  // The split solves: rows [0, csm) and [csm, n) are the two halves of the
+  // vector. Four streams like sf/sb, one per phase (forward over the first
+  // half, forward over the second, backward over the second, backward over
+  // the first): an entry's operand is the staged half in shared memory
+  // (column relative to the half) or, with kGlobalOperand set, the finished
+  // other half in global memory (absolute column); row ends are relative to
+  // the half.
+  int csm = 0;
+  std::vector<int32_t> csf_a, csf_b, csb_b, csb_a;
+
   // Triangular-solve streams (entries (x, y), padded to whole chunks):
   // forward over rows 0..n-1, backward over rows n-1..0.
   //   update (y >= 0):              acc -= lu[x] * v[y]

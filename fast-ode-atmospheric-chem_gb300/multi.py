@@ -67,7 +67,7 @@ class Part:
 
     def smem_per_block(self) -> int:
         lanes = ((self.max_cells + 31) // 32) * 32
-        return 8 * (32 + self.plan.info["smem_doubles_per_cell"] * lanes)
+        return 8 * (32 + self.plan.smem_items(getattr(self.alg, "kernel", "pipelined")) * lanes)
 
     def reset(self):
         self.Y.copy_(self.Y0)

@@ -85,6 +85,12 @@ class Plan:
     def has_constraints(self) -> bool:
         return bool(np.any(self.mass == 0.0))
 
+    def smem_items(self, kernel: str = "pipelined") -> int:
+        """Shared-memory doubles per cell of a block running ``kernel``."""
+        if kernel == "compact":
+            return int(self.info["compact_smem_doubles_per_cell"])
+        return int(self.info["smem_doubles_per_cell"])
+
     def workspace_bytes(self, slots: int, max_group_cells: int) -> int:
         out = C.c_size_t()
         _abi.check(_abi.lib().fo_workspace_bytes(self.handle, int(slots), int(max_group_cells), C.byref(out)),

@@ -31,9 +31,17 @@ class TuneResult:
     table: list = field(default_factory=list)   # (config, cell-intervals/s or None when it does not fit)
 
 
-def fits(smem_doubles_per_cell: int, group_size: int) -> bool:
+def _items(smem_doubles_per_cell, kernel: str) -> int:
+    """Shared-memory doubles per cell: one figure for every kernel, or a dict
+    kernel -> figure (the compact kernel needs about half)."""
+    if isinstance(smem_doubles_per_cell, dict):
+        return smem_doubles_per_cell[kernel]
+    return smem_doubles_per_cell
+
+
+def fits(smem_doubles_per_cell, group_size: int, kernel: str = "pipelined") -> bool:
     lanes = ((group_size + 31) // 32) * 32
-    return 8 * (32 + smem_doubles_per_cell * lanes) <= SMEM_LIMIT
+    return 8 * (32 + _items(smem_doubles_per_cell, kernel) * lanes) <= SMEM_LIMIT
 
 
 def candidates(smem_doubles_per_cell: int, group_sizes=(16, 32, 64, 128),
@@ -53,7 +61,7 @@ def autotune(measure, smem_doubles_per_cell: int, configs=None) -> TuneResult:
     table = []
     best, best_v = None, -1.0
     for c in configs:
-        if not fits(smem_doubles_per_cell, c.group_size):
+        if not fits(smem_doubles_per_cell, c.group_size, c.kernel):
             table.append((c, None))
             continue
         v = float(measure(c))
@@ -84,7 +92,7 @@ def measure_on_device(mech, Y0, k_of, dt, atol, rtol, warm: int = 1, timed: int 
         b = Batch(mech, Y0, group_size=c.group_size, algorithm=alg, mass=mass)
         if c.persistent:
             lanes = ((c.group_size + 31) // 32) * 32
-            per_sm = max(1, min(8, SMEM_LIMIT // (8 * (32 + b.plan.info["smem_doubles_per_cell"] * lanes))))
+            per_sm = max(1, min(8, SMEM_LIMIT // (8 * (32 + b.plan.smem_items(c.kernel) * lanes))))
             b = Batch(mech, Y0, group_size=c.group_size, algorithm=alg, mass=mass,
                       slots=torch.cuda.get_device_properties(b.plan.device).multi_processor_count * per_sm)
         for i in range(warm):

@@ -99,6 +99,7 @@ typedef struct fo_plan_info {
   int32_t stoich_nnz;         /* nonzeros of S */
   int64_t scratch_doubles_per_cell;  /* per-cell device scratch of the integrator */
   int32_t smem_doubles_per_cell;     /* per-cell shared memory of the integrator */
+  int32_t compact_smem_doubles_per_cell;  /* the same for FO_VARIANT_COMPACT */
 } fo_plan_info;
 
 typedef struct fo_plan fo_plan;  /* opaque */
@@ -155,6 +156,13 @@ typedef struct fo_options {
  * against. */
 #define FO_VARIANT_PIPELINED 0
 #define FO_VARIANT_PLAIN 1
+/* COMPACT eliminates every row in two passes over halves of its slots (the
+ * second pass reloads the first pass's multipliers) and solves with half the
+ * vector staged at a time, the other half in global memory, so a group needs
+ * about half the shared memory and twice as many groups stay resident per SM.
+ * The factors are those of PIPELINED bit for bit; the solves differ in
+ * summation order (roundoff). fo_adjoint_interval runs PIPELINED. */
+#define FO_VARIANT_COMPACT 2
 
 /* Host-only symbolic analysis: ordering, fill and flop counts, and (when
  * perm is not NULL) the elimination order perm[p] = species eliminated p-th.

@@ -56,13 +56,14 @@ def test_backward_euler_ts1_matches_reference(cuda, config):
     assert err.max() <= Y_TOL, err.max()
 
 
-def test_backward_euler_plain_kernel(cuda):
-    """The plain LU loops give the same Counts on the configuration with
-    failed steps."""
+@pytest.mark.parametrize("kernel", ["plain", "compact"])
+def test_backward_euler_other_kernels(cuda, kernel):
+    """The plain LU loops and the compact kernel give the same Counts on the
+    configuration with failed steps."""
     torch = cuda
     f = load("ts1_tier1_30s")
     b = load("ts1_tier1_30s_backward_euler")
-    batch, status = _run(torch, f, b, "be_it3", kernel="plain")
+    batch, status = _run(torch, f, b, "be_it3", kernel=kernel)
     np.testing.assert_array_equal(batch.counts.cpu().numpy().sum(axis=0), b["be_it3_counts"])
     np.testing.assert_array_equal(status, b["be_it3_status"])
     assert rel_err(batch.state(), b["be_it3_Y"]).max() <= Y_TOL

@@ -47,7 +47,7 @@ def run_batch(cuda, f, trace_cap=64, slots=0, group_size=None, kernel="pipelined
 
 
 @pytest.mark.parametrize("case", CASES)
-@pytest.mark.parametrize("kernel", ["pipelined", "plain"])
+@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact"])
 def test_device_matches_reference_fixture(cuda, case, kernel):
     f = load(case)
     b, statuses, traces = run_batch(cuda, f, kernel=kernel)
@@ -70,12 +70,13 @@ def test_device_matches_reference_fixture(cuda, case, kernel):
 
 
 @pytest.mark.parametrize("case", CASES)
-def test_persistent_queue_gives_the_same_bits(cuda, case):
+@pytest.mark.parametrize("kernel", ["pipelined", "compact"])
+def test_persistent_queue_gives_the_same_bits(cuda, case, kernel):
     """A persistent launch that pulls groups from the device queue computes
     exactly what one block per group computes."""
     f = load(case)
-    b0, s0, _ = run_batch(cuda, f, trace_cap=0)
-    b1, s1, _ = run_batch(cuda, f, trace_cap=0, slots=1)
+    b0, s0, _ = run_batch(cuda, f, trace_cap=0, kernel=kernel)
+    b1, s1, _ = run_batch(cuda, f, trace_cap=0, slots=1, kernel=kernel)
     np.testing.assert_array_equal(b0.state(), b1.state())
     np.testing.assert_array_equal(b0.counts.cpu().numpy(), b1.counts.cpu().numpy())
     np.testing.assert_array_equal(s0, s1)
@@ -128,16 +129,18 @@ def test_rhs_and_jacobian_match_oracle(cuda, case):
     assert np.all(np.abs(F - Fr) <= 1e-14 * scale + 1e-300)
 
 
-def test_ragged_groups_and_idle_lanes(cuda):
+@pytest.mark.parametrize("kernel", ["pipelined", "compact"])
+def test_ragged_groups_and_idle_lanes(cuda, kernel):
     """Groups of 20 and 12 cells (idle lanes in the warp) give the oracle's
     Counts and states for those groups."""
     from oracle import rosenbrock as O
+    from fastode_gb300 import Algorithm
     f = load("ros3_20x40")
     mech = mechanism_of(f)
     torch = cuda
     from fastode_gb300.batch import Batch
     offs = np.array([0, 20, 32, 64], dtype=np.int32)
-    b = Batch(mech, f["Y0"], offsets=offs)
+    b = Batch(mech, f["Y0"], offsets=offs, algorithm=Algorithm(kernel=kernel))
     atol = torch.from_numpy(f["atol"]).cuda()
     n_int = 5
     for i in range(n_int):

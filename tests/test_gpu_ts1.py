@@ -12,7 +12,7 @@ from golden_cases import load, rel_err, table_mechanism, ts1_k
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("kernel", ["pipelined", "plain"])
+@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact"])
 def test_ts1_tier1_counts_match_the_archive(cuda, kernel):
     from fastode_gb300 import Algorithm
     from fastode_gb300.batch import Batch

@@ -204,3 +204,54 @@ def test_backward_euler_options_and_validation():
     assert be.converged(np.array([[1e-7, 1e-13]]), Y, atol, 1e-6)
     assert not be.converged(np.array([[1e-5, 0.0]]), Y, atol, 1e-6)
     assert not be.converged(np.array([[np.nan, 0.0]]), Y, atol, 1e-6)
+
+
+def _write_descriptor(path, mech):
+    from fastode_gb300.chem import mechanism_tables
+    t = mechanism_tables(mech)
+    arrays = [np.array([t["n"], t["R"], t["P"]], dtype=np.int64), np.asarray(t["react"], np.int64),
+              np.asarray(t["s_indptr"], np.int32), np.asarray(t["s_idx"], np.int32), np.asarray(t["s_val"], np.float64),
+              np.asarray(t["rows"], np.int64), np.asarray(t["cols"], np.int64),
+              np.asarray(t["j_indptr"], np.int32), np.asarray(t["j_idx"], np.int32), np.asarray(t["j_val"], np.float64)]
+    with open(path, "wb") as fh:
+        for a in arrays:
+            fh.write(np.int64(a.size).tobytes())
+            fh.write(np.ascontiguousarray(a).tobytes())
+
+
+@pytest.fixture(scope="module")
+def compact_emulator(tmp_path_factory):
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    out = tmp_path_factory.mktemp("emu") / "compact_emulator"
+    csrc = ROOT / "fast-ode-atmospheric-chem_gb300" / "csrc"
+    subprocess.run([cxx, "-std=c++17", "-O2", f"-I{csrc}", f"-I{ROOT / 'include'}",
+                    str(ROOT / "tests" / "cpp" / "compact_emulator.cpp"), str(csrc / "symbolic.cpp"), "-o", str(out)],
+                   check=True)
+    return out
+
+
+@pytest.mark.parametrize("which", ["ros3_20x40", "ros3_210x500", "ts1", "dae", "60x40", "120x260"])
+def test_compact_tables_reproduce_the_plain_factorization(compact_emulator, tmp_path, which):
+    """The compact variant's two-pass elimination stream and split solves,
+    executed on the host over the tables the library builds, give the plain
+    row-by-row factorization bit for bit and its solution to roundoff."""
+    import subprocess
+    from fastode_gb300 import synthetic as syn
+    from golden_cases import table_mechanism
+    if which.startswith("ros3"):
+        mech = mechanism_of(load(which))
+    elif which == "ts1":
+        mech = table_mechanism(load("ts1_tier1_30s"))
+    elif which == "dae":
+        mech = syn.dae_constrained(n_cells=32, intervals=1).sm.mech
+    else:
+        mech = {"60x40": syn.batched_uneven(n_cells=96, intervals=1)[0],
+                "120x260": syn.batched_uneven(n_cells=96, intervals=1)[1]}[which].sm.mech
+    desc = tmp_path / "mech.bin"
+    _write_descriptor(desc, mech)
+    r = subprocess.run([str(compact_emulator), str(desc)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
