@@ -196,7 +196,7 @@ def run_ours(args, rank, world):
     thermal()
     Y0 = torch.from_numpy(cells.Y0).to(dev)
     from fastode_gb300 import Algorithm
-    batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel=args.kernel))
+    batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel=args.kernel, ordering=args.ordering))
 
     def reset(b=batch):
         b.Y.copy_(Y0.t())
@@ -233,7 +233,7 @@ def run_ours(args, rank, world):
     plain = None
     n_plain = min(args.plain_steps, args.steps)
     if n_plain > 0 and args.kernel != "plain":
-        pb = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel="plain"))
+        pb = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel="plain", ordering=args.ordering))
         torch.cuda.synchronize()
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         p0.record()
@@ -267,7 +267,7 @@ def run_ours(args, rank, world):
         from fastode_gb300.batch import HostState
         pinned_k = [torch.from_numpy(wl.k_at(i)).pin_memory() for i in range(e2e_steps)]
         Yh = torch.from_numpy(cells.Y0.copy()).pin_memory()
-        state = HostState(sm.mech, Cc, n, R, 32, Algorithm(kernel=args.kernel), None, args.slots, dev)
+        state = HostState(sm.mech, Cc, n, R, 32, Algorithm(kernel=args.kernel, ordering=args.ordering), None, args.slots, dev)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h2d = d2h = 0
@@ -312,6 +312,7 @@ def run_ours(args, rank, world):
         "e2e": e2e,
         "plain_gpu": plain,
         "kernel_variant": args.kernel,
+        "lu": {k: batch.plan.info[k] for k in ("ordering", "lu_fma", "nnz_lu", "solve_fma")},
         "interval_ms": {"first": interval_ms[0], "median": float(np.median(interval_ms)),
                         "max": float(max(interval_ms))},
     }
@@ -359,7 +360,7 @@ def run_batched(args):
     sp = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
     wls = syn.batched_uneven(n_cells=args.cells, intervals=args.steps)
     from fastode_gb300 import Algorithm
-    group_size, kernel, tuning = 32, "pipelined", None
+    group_size, kernel, tuning = 32, args.kernel, None
     if args.autotune:
         # the group size and kernel of the launch, measured on 4,096 cells of
         # the largest mechanism (one untimed and two timed intervals each)
@@ -380,7 +381,7 @@ def run_batched(args):
     for wl in wls:
         k, photo = _device_rates(lib, wl.sm, wl.cells, dev, sp)
         p = Part(wl.sm.mech, torch.from_numpy(wl.cells.Y0).to(dev), k.t(), wl.atol, wl.rtol, wl.dt,
-                 group_size=group_size, algorithm=Algorithm(kernel=kernel),
+                 group_size=group_size, algorithm=Algorithm(kernel=kernel, ordering=args.ordering),
                  photolysis=(photo, wl.sm.J[photo], wl.cells.phase))
         parts.append(p)
     fma_rate = C.c_double()
@@ -609,7 +610,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--cells", type=int, default=65536)
     ap.add_argument("--slots", type=int, default=0)
-    ap.add_argument("--kernel", default="pipelined", choices=["pipelined", "plain", "compact"])
+    ap.add_argument("--kernel", default="compact", choices=["compact", "pipelined", "plain"])
+    ap.add_argument("--ordering", default="auto", choices=["auto", "refined", "min_fill", "min_degree", "natural"],
+                    help="elimination order of the sparse LU (auto: the greedy orders refined by local search)")
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=12)

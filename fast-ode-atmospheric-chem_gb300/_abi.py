@@ -15,7 +15,7 @@ FO_E_INVALID, FO_E_CUDA, FO_E_UNSUPPORTED, FO_E_WORKSPACE, FO_E_ALLOC = -1, -2, 
 STATUS_STRINGS = ("converged", "too many steps", "step too small", "nan or inf", "projection failed",
                   "accepted unconverged")
 NUM_COUNTS = 13
-ORDERINGS = {"auto": 0, "natural": 1, "min_degree": 2, "min_fill": 3}
+ORDERINGS = {"auto": 0, "natural": 1, "min_degree": 2, "min_fill": 3, "refined": 4}
 ORDERING_NAMES = {v: k for k, v in ORDERINGS.items()}
 
 

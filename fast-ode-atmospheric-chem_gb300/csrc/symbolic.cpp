@@ -11,6 +11,7 @@
 #include "symbolic.h"
 
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <numeric>
 #include <queue>
@@ -195,6 +196,133 @@ int64_t cost_of(const fo_mechanism_desc& m, const std::vector<int>& order) {
   return symbolic_lu(m.n, permuted_pattern(m, iperm), nullptr, nullptr, nullptr);
 }
 
+// The LU FMA count of an elimination order, by bitset symbolic elimination,
+// for the many evaluations of the local search below. Row i's pattern is its
+// own united with U(k) for each k < i in it, taken in increasing k (merging
+// U(k) only adds columns above k, so one ascending scan finds them all).
+class FmaCounter {
+ public:
+  explicit FmaCounter(const fo_mechanism_desc& m) : n_(m.n), words_((m.n + 63) / 64), nnz_(m.nnz), pat_(m.n) {
+    for (int e = 0; e < m.nnz; ++e) pat_[m.pat_rows[e]].push_back((int)m.pat_cols[e]);
+    for (int i = 0; i < n_; ++i) pat_[i].push_back(i);
+    rows_.assign((size_t)n_ * words_, 0);
+    upper_.assign((size_t)n_ * words_, 0);
+    ucount_.assign(n_, 0);
+    pos_.assign(n_, 0);
+  }
+  // Stops early, returning a count >= limit, once the count reaches limit.
+  int64_t count(const std::vector<int>& order, int64_t limit) {
+    const int W = words_;
+    for (int p = 0; p < n_; ++p) pos_[order[p]] = p;
+    std::fill(rows_.begin(), rows_.end(), 0ull);
+    for (int v = 0; v < n_; ++v) {
+      uint64_t* r = &rows_[(size_t)pos_[v] * W];
+      for (int c : pat_[v]) r[pos_[c] >> 6] |= 1ull << (pos_[c] & 63);
+    }
+    int64_t fma = 0;
+    for (int i = 0; i < n_; ++i) {
+      uint64_t* row = &rows_[(size_t)i * W];
+      const int iw = i >> 6, ib = i & 63;
+      for (int w = 0; w <= iw; ++w) {
+        const uint64_t below_i = w < iw ? ~0ull : ((1ull << ib) - 1);
+        uint64_t unseen = ~0ull;
+        for (;;) {
+          const uint64_t x = row[w] & below_i & unseen;
+          if (!x) break;
+          const int b = __builtin_ctzll(x);
+          const int k = w * 64 + b;
+          unseen = b == 63 ? 0ull : ~((2ull << b) - 1);
+          fma += ucount_[k];
+          const uint64_t* uk = &upper_[(size_t)k * W];
+          for (int u = w; u < W; ++u) row[u] |= uk[u];
+        }
+      }
+      uint64_t* ui = &upper_[(size_t)i * W];
+      int c = 0;
+      for (int u = 0; u < W; ++u) {
+        const uint64_t x = u < iw ? 0ull : u > iw ? row[u] : (ib == 63 ? 0ull : row[u] & ~((2ull << ib) - 1));
+        ui[u] = x;
+        c += popcnt(x);
+      }
+      ucount_[i] = c;
+      if (fma >= limit) return fma;
+    }
+    return fma;
+  }
+  // Word operations of one evaluation, for sizing the search.
+  int64_t work(const std::vector<int>& order) {
+    count(order, INT64_MAX);
+    int64_t l = 0;
+    for (int i = 0; i < n_; ++i) l += ucount_[i];
+    return (int64_t)n_ * words_ + nnz_ + l * words_;
+  }
+
+ private:
+  int n_, words_;
+  int64_t nnz_;
+  std::vector<std::vector<int>> pat_;
+  std::vector<uint64_t> rows_, upper_;
+  std::vector<int> ucount_, pos_;
+};
+
+// splitmix64: a fixed, portable pseudo-random stream.
+struct SplitMix {
+  uint64_t s;
+  uint64_t next() {
+    uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+  }
+  int below(int n) { return (int)(next() % (uint64_t)n); }
+};
+
+// Local search on the elimination order by threshold accepting: move one
+// species to another position and keep the move while the LU FMA count stays
+// below the current count plus a threshold that falls linearly from 0.3% of
+// the starting count to zero. The greedy orders above minimise fill one
+// elimination at a time; on the random-graph patterns of large mechanisms
+// this finds orders with about half their FMAs. Integer arithmetic and a
+// fixed seed make the order the same on every host. The number of moves is
+// capped by an operation budget (about a second for 210 species).
+std::vector<int> refine_order(const fo_mechanism_desc& m, const std::vector<int>& start, int64_t* cost) {
+  const int n = m.n;
+  if (n < 3) {
+    *cost = cost_of(m, start);
+    return start;
+  }
+  FmaCounter counter(m);
+  const int64_t kWorkBudget = 600000000;
+  const int64_t moves = std::max<int64_t>(1000, std::min<int64_t>(20000, kWorkBudget / std::max<int64_t>(1, counter.work(start))));
+  std::vector<int> order = start, best = start, trial(n);
+  int64_t cur = counter.count(start, INT64_MAX), best_cost = cur;
+  const int64_t t0 = cur * 3 / 1000;
+  SplitMix rng{0x5eedf00dull};
+  for (int64_t e = 0; e < moves; ++e) {
+    const int64_t threshold = t0 - t0 * e / moves;
+    const int i = rng.below(n), j = rng.below(n);
+    if (i == j) continue;
+    trial = order;
+    const int v = trial[i];
+    if (i < j)
+      for (int q = i; q < j; ++q) trial[q] = trial[q + 1];
+    else
+      for (int q = i; q > j; --q) trial[q] = trial[q - 1];
+    trial[j] = v;
+    const int64_t c = counter.count(trial, cur + threshold);
+    if (c < cur + threshold) {
+      order.swap(trial);
+      cur = c;
+      if (cur < best_cost) {
+        best_cost = cur;
+        best = order;
+      }
+    }
+  }
+  *cost = best_cost;
+  return best;
+}
+
 }  // namespace
 
 // The compact variant's tables (see HostTables), built from the LU structure
@@ -315,12 +443,12 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
   std::vector<int> natural(n);
   std::iota(natural.begin(), natural.end(), 0);
   std::vector<std::pair<int, std::vector<int>>> cands;
-  if (ordering == FO_ORDER_NATURAL || ordering == FO_ORDER_AUTO) cands.push_back({FO_ORDER_NATURAL, natural});
-  if (ordering == FO_ORDER_MIN_DEGREE || ordering == FO_ORDER_AUTO)
-    cands.push_back({FO_ORDER_MIN_DEGREE, greedy_order(n, adj, 0, 0)});
-  if (ordering == FO_ORDER_MIN_FILL || ordering == FO_ORDER_AUTO) {
+  const bool every = ordering == FO_ORDER_AUTO || ordering == FO_ORDER_REFINED;
+  if (ordering == FO_ORDER_NATURAL || every) cands.push_back({FO_ORDER_NATURAL, natural});
+  if (ordering == FO_ORDER_MIN_DEGREE || every) cands.push_back({FO_ORDER_MIN_DEGREE, greedy_order(n, adj, 0, 0)});
+  if (ordering == FO_ORDER_MIN_FILL || every) {
     cands.push_back({FO_ORDER_MIN_FILL, greedy_order(n, adj, 1, n <= 400 ? n : 32)});
-    if (ordering == FO_ORDER_AUTO && n > 8) cands.push_back({FO_ORDER_MIN_FILL, greedy_order(n, adj, 1, 8)});
+    if (every && n > 8) cands.push_back({FO_ORDER_MIN_FILL, greedy_order(n, adj, 1, 8)});
   }
   if (cands.empty()) return "unknown ordering";
   int best = 0;
@@ -333,7 +461,16 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
     }
   }
   t->ordering = cands[best].first;
-  t->perm.assign(cands[best].second.begin(), cands[best].second.end());
+  std::vector<int> chosen = cands[best].second;
+  if (every) {
+    int64_t refined_cost = 0;
+    std::vector<int> refined = refine_order(m, chosen, &refined_cost);
+    if (refined_cost < best_cost || ordering == FO_ORDER_REFINED) {
+      chosen = refined;
+      t->ordering = FO_ORDER_REFINED;
+    }
+  }
+  t->perm.assign(chosen.begin(), chosen.end());
   t->iperm.assign(n, 0);
   for (int p = 0; p < n; ++p) t->iperm[t->perm[p]] = p;
 

@@ -20,7 +20,7 @@ SMEM_LIMIT = 232448
 
 @dataclass(frozen=True)
 class Config:
-    kernel: str = "pipelined"     # FO_VARIANT_*
+    kernel: str = "compact"       # FO_VARIANT_*
     group_size: int = 32
     persistent: bool = False      # one block per group, or persistent blocks pulling a queue
 
@@ -45,7 +45,7 @@ def fits(smem_doubles_per_cell, group_size: int, kernel: str = "pipelined") -> b
 
 
 def candidates(smem_doubles_per_cell: int, group_sizes=(16, 32, 64, 128),
-               kernels=("pipelined", "plain"), persistent=(False, True)) -> list:
+               kernels=("compact", "pipelined", "plain"), persistent=(False, True)) -> list:
     out = []
     for k in kernels:
         for g in group_sizes:

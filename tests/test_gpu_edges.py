@@ -82,14 +82,16 @@ def test_zero_groups_and_invalid_arguments(cuda):
 
 
 def test_group_too_large_for_shared_memory_is_rejected(cuda):
-    """210 species x 256 cells of work row do not fit in one block's shared
-    memory: the call fails with FO_E_UNSUPPORTED instead of launching."""
-    from fastode_gb300 import _abi
+    """210 species x 256 cells of whole work rows (the pipelined kernel) do
+    not fit in one block's shared memory: the call fails with
+    FO_E_UNSUPPORTED instead of launching. (The compact kernel's half rows
+    do fit.)"""
+    from fastode_gb300 import Algorithm, _abi
     from fastode_gb300.batch import Batch
     f = load("ros3_210x500")
     mech = mechanism_of(f)
     Y0 = np.repeat(f["Y0"], 4, axis=0)                       # 256 cells
-    b = Batch(mech, Y0, group_size=256)
+    b = Batch(mech, Y0, group_size=256, algorithm=Algorithm(kernel="pipelined"))
     torch = cuda
     k = torch.from_numpy(np.ascontiguousarray(np.repeat(f["k"][0], 4, axis=0).T)).cuda()
     atol = torch.from_numpy(f["atol"]).cuda()

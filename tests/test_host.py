@@ -121,7 +121,7 @@ def structural_lu(n, rows, cols, perm):
 
 
 @pytest.mark.parametrize("case", CASES)
-@pytest.mark.parametrize("ordering", ["natural", "min_degree", "min_fill", "auto"])
+@pytest.mark.parametrize("ordering", ["natural", "min_degree", "min_fill", "auto", "refined"])
 def test_symbolic_analysis_matches_dense_elimination(built_library, case, ordering):
     from fastode_gb300.plan import analyze
     mech = mechanism_of(load(case))
@@ -140,6 +140,19 @@ def test_auto_ordering_is_the_cheapest(built_library):
     costs = {o: analyze(mech, o)["lu_fma"] for o in ("natural", "min_degree", "min_fill")}
     assert analyze(mech, "auto")["lu_fma"] <= min(costs.values())
     assert costs["min_degree"] < costs["natural"]
+
+
+def test_refined_ordering_is_deterministic_and_cheaper(built_library):
+    """The local search on the elimination order gives the same order on every
+    call, and on the 210-species mechanism it removes well over a quarter of
+    the greedy orders' LU FMAs."""
+    from fastode_gb300.plan import analyze
+    mech = mechanism_of(load("ros3_210x500"))
+    a, b = analyze(mech, "refined"), analyze(mech, "refined")
+    np.testing.assert_array_equal(a["perm"], b["perm"])
+    greedy = min(analyze(mech, o)["lu_fma"] for o in ("natural", "min_degree", "min_fill"))
+    assert a["lu_fma"] <= 0.7 * greedy, (a["lu_fma"], greedy)
+    assert analyze(mech, "auto")["lu_fma"] == a["lu_fma"]
 
 
 def test_analysis_rejects_bad_descriptors(built_library):
