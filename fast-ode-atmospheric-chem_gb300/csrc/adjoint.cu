@@ -230,7 +230,7 @@ __device__ __forceinline__ void fixed_step(const AdjParams& a, const Lane& ln, d
   attempt(p, ln, h, y, ynew, scr, w, cr, cs, U);
 }
 
-__global__ void __launch_bounds__(256) adjoint_kernel(AdjParams a) {
+__global__ void __maxnreg__(255) adjoint_kernel(AdjParams a) {
   extern __shared__ double smem[];
   double* red = smem;
   double* w = smem + 32;

@@ -27,7 +27,12 @@
 
 namespace fo {
 
-__global__ void __launch_bounds__(256) solve_kernel(SolveParams p) {
+// __maxnreg__(255): a block of at most 256 threads still fits one SM's
+// register file, and eight single-warp groups per SM (the compact kernel's
+// shared-memory limit) fit too. Left to itself ptxas gave this kernel 128
+// registers, and the triangular solves' register-buffered chunks paid for it
+// (one interval of 65,536 cells took 18% longer).
+__global__ void __maxnreg__(255) solve_kernel(SolveParams p) {
   extern __shared__ double smem[];
   double* red = smem;       // 32 doubles
   double* w = smem + 32;    // n * lanes
@@ -93,7 +98,7 @@ cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream
 // Several mechanisms in one persistent launch: the batch table lives in the
 // workspace, items [starts[b], starts[b+1]) of the queue are the groups of
 // batch b, and each block integrates whatever group it pulls next.
-__global__ void __launch_bounds__(256) solve_multi_kernel(const SolveParams* __restrict__ batches, int nb,
+__global__ void __maxnreg__(255) solve_multi_kernel(const SolveParams* __restrict__ batches, int nb,
                                                           const int32_t* __restrict__ starts, int32_t* queue,
                                                           double* scratch, int64_t slot_doubles) {
   extern __shared__ double smem[];

@@ -196,10 +196,16 @@ int64_t cost_of(const fo_mechanism_desc& m, const std::vector<int>& order) {
   return symbolic_lu(m.n, permuted_pattern(m, iperm), nullptr, nullptr, nullptr);
 }
 
-// The LU FMA count of an elimination order, by bitset symbolic elimination,
-// for the many evaluations of the local search below. Row i's pattern is its
-// own united with U(k) for each k < i in it, taken in increasing k (merging
-// U(k) only adds columns above k, so one ascending scan finds them all).
+// The cost of an elimination order for the local search below: the
+// elimination's FMAs plus kEntryWeight per LU entry, since every attempt also
+// runs three stage solves that touch each entry once. With weight 4 the search
+// on the 210-species mechanism keeps its FMA count and finds orders with
+// about 9% fewer entries; larger weights trade FMAs for entries.
+// Counted by bitset symbolic elimination: row i's pattern is its own united
+// with U(k) for each k < i in it, taken in increasing k (merging U(k) only
+// adds columns above k, so one ascending scan finds them all).
+constexpr int64_t kEntryWeight = 4;
+
 class FmaCounter {
  public:
   explicit FmaCounter(const fo_mechanism_desc& m) : n_(m.n), words_((m.n + 63) / 64), nnz_(m.nnz), pat_(m.n) {
@@ -245,6 +251,9 @@ class FmaCounter {
         c += popcnt(x);
       }
       ucount_[i] = c;
+      int entries = 0;
+      for (int u = 0; u < W; ++u) entries += popcnt(row[u]);
+      fma += kEntryWeight * entries;
       if (fma >= limit) return fma;
     }
     return fma;
@@ -278,24 +287,24 @@ struct SplitMix {
 };
 
 // Local search on the elimination order by threshold accepting: move one
-// species to another position and keep the move while the LU FMA count stays
-// below the current count plus a threshold that falls linearly from 0.3% of
-// the starting count to zero. The greedy orders above minimise fill one
+// species to another position and keep the move while the cost above stays
+// below the current cost plus a threshold that falls linearly from 0.3% of
+// the starting cost to zero. The greedy orders above minimise fill one
 // elimination at a time; on the random-graph patterns of large mechanisms
 // this finds orders with about half their FMAs. Integer arithmetic and a
 // fixed seed make the order the same on every host. The number of moves is
-// capped by an operation budget (about a second for 210 species).
-std::vector<int> refine_order(const fo_mechanism_desc& m, const std::vector<int>& start, int64_t* cost) {
+// capped by an operation budget (about a second for 210 species). Returns
+// the best order found; *improved tells whether it is cheaper than start.
+std::vector<int> refine_order(const fo_mechanism_desc& m, const std::vector<int>& start, bool* improved) {
   const int n = m.n;
-  if (n < 3) {
-    *cost = cost_of(m, start);
-    return start;
-  }
+  *improved = false;
+  if (n < 3) return start;
   FmaCounter counter(m);
   const int64_t kWorkBudget = 600000000;
   const int64_t moves = std::max<int64_t>(1000, std::min<int64_t>(20000, kWorkBudget / std::max<int64_t>(1, counter.work(start))));
   std::vector<int> order = start, best = start, trial(n);
   int64_t cur = counter.count(start, INT64_MAX), best_cost = cur;
+  const int64_t start_cost = cur;
   const int64_t t0 = cur * 3 / 1000;
   SplitMix rng{0x5eedf00dull};
   for (int64_t e = 0; e < moves; ++e) {
@@ -319,7 +328,7 @@ std::vector<int> refine_order(const fo_mechanism_desc& m, const std::vector<int>
       }
     }
   }
-  *cost = best_cost;
+  *improved = best_cost < start_cost;
   return best;
 }
 
@@ -463,9 +472,9 @@ std::string build_tables(const fo_mechanism_desc& m, int ordering, HostTables* t
   t->ordering = cands[best].first;
   std::vector<int> chosen = cands[best].second;
   if (every) {
-    int64_t refined_cost = 0;
-    std::vector<int> refined = refine_order(m, chosen, &refined_cost);
-    if (refined_cost < best_cost || ordering == FO_ORDER_REFINED) {
+    bool improved = false;
+    std::vector<int> refined = refine_order(m, chosen, &improved);
+    if (improved || ordering == FO_ORDER_REFINED) {
       chosen = refined;
       t->ordering = FO_ORDER_REFINED;
     }
