@@ -337,11 +337,12 @@ __device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln,
 // pass A is the elimination restricted to the row's leading columns and
 // stores its multipliers as it makes them; pass B applies every multiplier's
 // updates of the trailing columns, in the same order, reloading A's
-// multipliers from the LU storage with an ordinary load (this thread stored
-// them; an asynchronous copy would not be ordered after that store). The
-// work row therefore holds half a row, and the factors are the pipelined
-// ones bit for bit. The U operands are staged one chunk ahead in a two-slot
-// ring: with twice as many groups resident per SM, a deeper ring buys nothing.
+// multipliers from the LU storage through the same ring as the U operands (a
+// block-scope fence between the passes orders this thread's stores of them
+// before the asynchronous copies that read them back). The work row therefore
+// holds half a row, and the factors are the pipelined ones bit for bit. The
+// operands are staged one chunk ahead in a two-slot ring: with twice as many
+// groups resident per SM, a deeper ring buys nothing.
 
 __device__ __noinline__ void factor_compact(const SolveParams& p, const Lane& ln, double alpha, const double* negj,
                                             double* lu, double* w, bool alg_only) {
@@ -371,6 +372,7 @@ __device__ __noinline__ void factor_compact(const SolveParams& p, const Lane& ln
       double* qlu = lu + (int64_t)(q0 + base) * L;     // this pass's slot s stands for lu[q0 + base + s]
       double l = 0.0;
       Meta mc, mi;
+      if (pass) __threadfence_block();   // pass A's stores before pass B's copies read them
       if (nch > 0) {
         meta_load(meta, mc);
         ring_issue(mc, lu, L, lane, ring);
@@ -399,7 +401,7 @@ __device__ __noinline__ void factor_compact(const SolveParams& p, const Lane& ln
             l = wv[s] * rs[s * L + lane];
             SCR(qlu, y) = l;
           } else if (y == kReloadSlot) {
-            l = lu[(int64_t)(word >> 16) * L + lane];
+            l = rs[s * L + lane];
           } else if (y != 0x7fffu) {
             wv[s] = fma(-l, rs[s * L + lane], wv[s]);
           }
@@ -420,15 +422,15 @@ __device__ __noinline__ void factor_compact(const SolveParams& p, const Lane& ln
 }
 
 // Forward and backward substitution driven by the solve streams
-// (symbolic.h): the factor entries are loaded one chunk ahead of their use
-// (they do not depend on the solution), the solution entries are read from
-// shared memory when the chunk computes.
+// (symbolic.h): a chunk's metadata is loaded two chunks ahead of its use and
+// its factor entries one chunk ahead (neither depends on the solution), so the
+// entries' loads never wait for their positions; the solution entries are read
+// from shared memory when the chunk computes. kMixed: an operand may lie in
+// the other, finished half of the vector in global memory (kGlobalOperand).
 template <bool kMixed>
-__device__ __forceinline__ void solve_load(const int2* __restrict__ meta, const double* __restrict__ lu,
-                                           const double* xg, int L, int lane, int4 (&m)[kChunk / 2],
-                                           double (&v)[kChunk], double (&g)[kChunk]) {
-#pragma unroll
-  for (int s = 0; s < kChunk / 2; ++s) m[s] = __ldg(reinterpret_cast<const int4*>(meta) + s);
+__device__ __forceinline__ void solve_values(const int4 (&m)[kChunk / 2], const double* __restrict__ lu,
+                                             const double* xg, int L, int lane, double (&v)[kChunk],
+                                             double (&g)[kChunk]) {
 #pragma unroll
   for (int s = 0; s < kChunk / 2; ++s) {
     const int p0 = m[s].x >= 0 ? m[s].x : -1 - m[s].x;
@@ -436,12 +438,16 @@ __device__ __forceinline__ void solve_load(const int2* __restrict__ meta, const 
     v[2 * s] = lu[(int64_t)p0 * L + lane];
     v[2 * s + 1] = lu[(int64_t)p1 * L + lane];
     if (kMixed) {
-      // an operand of the other, finished half of the vector (global memory)
       const int y0 = m[s].y, y1 = m[s].w;
       g[2 * s] = (y0 >= 0 && (y0 & kGlobalOperand)) ? xg[(int64_t)(y0 & ~kGlobalOperand) * L + lane] : 0.0;
       g[2 * s + 1] = (y1 >= 0 && (y1 & kGlobalOperand)) ? xg[(int64_t)(y1 & ~kGlobalOperand) * L + lane] : 0.0;
     }
   }
+}
+
+__device__ __forceinline__ void solve_meta(const int2* __restrict__ meta, int4 (&m)[kChunk / 2]) {
+#pragma unroll
+  for (int s = 0; s < kChunk / 2; ++s) m[s] = __ldg(reinterpret_cast<const int4*>(meta) + s);
 }
 
 // Four partial sums per row, entry s of a chunk feeding sum s mod 4: the
@@ -475,19 +481,31 @@ __device__ __forceinline__ void solve_compute(const int4 (&m)[kChunk / 2], const
 template <bool kBackward, bool kMixed = false>
 __device__ void solve_stream(const int2* __restrict__ st, int nst, const double* lu, double* w, int L, int lane,
                              const double* xg = nullptr) {
-  int4 mA[kChunk / 2], mB[kChunk / 2];
-  double vA[kChunk], vB[kChunk], gA[kChunk], gB[kChunk];
+  int4 mc[kChunk / 2], mn[kChunk / 2];
+  double vc[kChunk], gc[kChunk];
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   const int nch = nst / kChunk;
   if (nch == 0) return;            // an empty half (a one-species system)
-  solve_load<kMixed>(st, lu, xg, L, lane, mA, vA, gA);
+  solve_meta(st, mc);
+  solve_values<kMixed>(mc, lu, xg, L, lane, vc, gc);
+  if (nch > 1) solve_meta(st + kChunk, mn);
 #pragma unroll 1
-  for (int c = 0; c < nch; c += 2) {
-    if (c + 1 < nch) solve_load<kMixed>(st + (c + 1) * kChunk, lu, xg, L, lane, mB, vB, gB);
-    solve_compute<kBackward, kMixed>(mA, vA, gA, w, L, lane, acc);
-    if (c + 1 >= nch) break;
-    if (c + 2 < nch) solve_load<kMixed>(st + (c + 2) * kChunk, lu, xg, L, lane, mA, vA, gA);
-    solve_compute<kBackward, kMixed>(mB, vB, gB, w, L, lane, acc);
+  for (int c = 0; c < nch; ++c) {
+    int4 mnn[kChunk / 2];
+    double vn[kChunk], gn[kChunk];
+    if (c + 1 < nch) solve_values<kMixed>(mn, lu, xg, L, lane, vn, gn);
+    if (c + 2 < nch) solve_meta(st + (c + 2) * kChunk, mnn);
+    solve_compute<kBackward, kMixed>(mc, vc, gc, w, L, lane, acc);
+#pragma unroll
+    for (int s = 0; s < kChunk / 2; ++s) {
+      mc[s] = mn[s];
+      mn[s] = mnn[s];
+    }
+#pragma unroll
+    for (int s = 0; s < kChunk; ++s) {
+      vc[s] = vn[s];
+      gc[s] = gn[s];
+    }
   }
 }
 
