@@ -277,9 +277,10 @@ __device__ __forceinline__ void chunk_write(const Meta& m, double* w, int L, int
   }
 }
 
+template <int kL>
 __device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln, double alpha, const double* negj,
                                            double* lu, double* w, bool alg_only) {
-  const int L = ln.L, lane = ln.lane;
+  const int L = kL ? kL : ln.L, lane = ln.lane;
   const int n = p.t.n;
   const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
   const int32_t* __restrict__ diag = p.t.lu_diag;
@@ -344,9 +345,10 @@ __device__ __noinline__ void factor_stream(const SolveParams& p, const Lane& ln,
 // operands are staged one chunk ahead in a two-slot ring: with twice as many
 // groups resident per SM, a deeper ring buys nothing.
 
+template <int kL>
 __device__ __noinline__ void factor_compact(const SolveParams& p, const Lane& ln, double alpha, const double* negj,
                                             double* lu, double* w, bool alg_only) {
-  const int L = ln.L, lane = ln.lane;
+  const int L = kL ? kL : ln.L, lane = ln.lane;
   const int n = p.t.n;
   const int32_t* __restrict__ rowp = p.t.lu_row_ptr;
   const int32_t* __restrict__ diag = p.t.lu_diag;
@@ -479,7 +481,8 @@ __device__ __forceinline__ void solve_compute(const int4 (&m)[kChunk / 2], const
 
 // kMixed: the stream's operands may lie in xg (kGlobalOperand set).
 template <bool kBackward, bool kMixed = false>
-__device__ void solve_stream(const int2* __restrict__ st, int nst, const double* lu, double* w, int L, int lane,
+__device__ __forceinline__ void solve_stream(const int2* __restrict__ st, int nst, const double* lu, double* w, int L,
+                                             int lane,
                              const double* xg = nullptr) {
   int4 mc[kChunk / 2], mn[kChunk / 2];
   double vc[kChunk], gc[kChunk];
@@ -509,9 +512,11 @@ __device__ void solve_stream(const int2* __restrict__ st, int nst, const double*
   }
 }
 
+template <int kL>
 __device__ __noinline__ void lu_solve_pipelined(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
-  solve_stream<false>(p.t.sf, p.t.nsf, lu, w, ln.L, ln.lane);
-  solve_stream<true>(p.t.sb, p.t.nsb, lu, w, ln.L, ln.lane);
+  const int L = kL ? kL : ln.L;
+  solve_stream<false>(p.t.sf, p.t.nsf, lu, w, L, ln.lane);
+  solve_stream<true>(p.t.sb, p.t.nsb, lu, w, L, ln.lane);
 }
 
 // The compact solves: b and x are per-lane vectors in global memory (they may
@@ -520,9 +525,10 @@ __device__ __noinline__ void lu_solve_pipelined(const SolveParams& p, const Lane
 // forward over rows [csm, n) then reads it from x, as does nothing else until
 // backward over rows [n-1, csm) has finished the second half, which is stored
 // for backward over rows [csm-1, 0) to read.
-__device__ __noinline__ void lu_solve_compact(const SolveParams& p, const Lane& ln, const double* lu, double* w,
-                                              const double* b, double* x) {
-  const int L = ln.L, lane = ln.lane;
+template <int kL>
+__device__ __noinline__ void lu_solve_compact_l(const SolveParams& p, const Lane& ln, const double* lu, double* w,
+                                                const double* b, double* x) {
+  const int L = kL ? kL : ln.L, lane = ln.lane;
   const int n = p.t.n, m = p.t.csm;
   for (int i = 0; i < m; ++i) WROW(i) = SCR(b, i);
   solve_stream<false>(p.t.csf_a, p.t.ncsf_a, lu, w, L, lane);
@@ -534,6 +540,15 @@ __device__ __noinline__ void lu_solve_compact(const SolveParams& p, const Lane& 
   for (int i = 0; i < m; ++i) WROW(i) = SCR(x, i);
   solve_stream<true, true>(p.t.csb_a, p.t.ncsb_a, lu, w, L, lane, x);
   for (int i = 0; i < m; ++i) SCR(x, i) = WROW(i);
+}
+
+// The stream kernels specialised for 32 lanes (one warp per group, the usual
+// launch) fold the lane stride into immediate offsets; other group sizes run
+// the general instantiation.
+__device__ __forceinline__ void lu_solve_compact(const SolveParams& p, const Lane& ln, const double* lu, double* w,
+                                                 const double* b, double* x) {
+  if (ln.L == 32) lu_solve_compact_l<32>(p, ln, lu, w, b, x);
+  else lu_solve_compact_l<0>(p, ln, lu, w, b, x);
 }
 
 // Forward and backward substitution in place on w (fastode/linalg.py:80-81).
@@ -560,13 +575,19 @@ __device__ void lu_solve(const SolveParams& p, const Lane& ln, const double* lu,
 __device__ void factor_any(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
                            double* w, bool alg_only) {
   if (p.o.variant == FO_VARIANT_PLAIN) factor(p, ln, alpha, negj, lu, w, alg_only);
-  else if (p.o.variant == FO_VARIANT_COMPACT) factor_compact(p, ln, alpha, negj, lu, w, alg_only);
-  else factor_stream(p, ln, alpha, negj, lu, w, alg_only);
+  else if (p.o.variant == FO_VARIANT_COMPACT) {
+    if (ln.L == 32) factor_compact<32>(p, ln, alpha, negj, lu, w, alg_only);
+    else factor_compact<0>(p, ln, alpha, negj, lu, w, alg_only);
+  } else {
+    if (ln.L == 32) factor_stream<32>(p, ln, alpha, negj, lu, w, alg_only);
+    else factor_stream<0>(p, ln, alpha, negj, lu, w, alg_only);
+  }
 }
 
 __device__ __forceinline__ void solve_in_w(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
   if (p.o.variant == FO_VARIANT_PLAIN) lu_solve(p, ln, lu, w);
-  else lu_solve_pipelined(p, ln, lu, w);
+  else if (ln.L == 32) lu_solve_pipelined<32>(p, ln, lu, w);
+  else lu_solve_pipelined<0>(p, ln, lu, w);
 }
 
 // x = A^-1 b with the factors in lu (b and x per-lane vectors, may alias).

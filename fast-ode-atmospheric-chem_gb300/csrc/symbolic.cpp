@@ -362,6 +362,33 @@ void build_compact(HostTables* t) {
   auto place = [&](int slot) {
     while (touched[slot] >= entries() / kStreamChunk) pad_chunk();
   };
+  // A multiplier's updates, in any order (each touches its own slot, and a
+  // slot still receives its updates in multiplier order, so the factors do not
+  // change): each next entry is the first pending update whose slot the
+  // current chunk has not touched; the chunk is padded only when none is left.
+  std::vector<std::pair<int, int>> group;  // (slot relative to the pass, LU position of the U entry)
+  auto emit_group = [&]() {
+    size_t done = 0;
+    while (done < group.size()) {
+      const int64_t chunk = entries() / kStreamChunk;
+      size_t pick = group.size();
+      for (size_t i = done; i < group.size(); ++i)
+        if (touched[group[i].first] < chunk) {
+          pick = i;
+          break;
+        }
+      if (pick == group.size()) {
+        pad_chunk();
+        continue;
+      }
+      std::swap(group[done], group[pick]);
+      const int y = group[done].first, u = group[done].second;
+      touched[y] = chunk;
+      t->cep.push_back(((uint32_t)u << 16) | (uint32_t)y);
+      ++done;
+    }
+    group.clear();
+  };
   for (int r = 0; r < n; ++r) {
     const int q0 = t->lu_row_ptr[r], len = t->lu_row_ptr[r + 1] - q0, dg = t->lu_diag[r];
     const int split = (len + 1) / 2;
@@ -388,10 +415,9 @@ void build_compact(HostTables* t) {
             t->cep.push_back(((uint32_t)q << 16) | kReloadSlot);
             opened = true;
           }
-          place(y - base);
-          touched[y - base] = entries() / kStreamChunk;
-          t->cep.push_back(((uint32_t)u << 16) | (uint32_t)(y - base));
+          group.push_back({y - base, u});
         }
+        emit_group();
       }
       pad();
       t->ce_ptr.push_back((int32_t)t->cep.size());
