@@ -97,3 +97,25 @@ def test_group_too_large_for_shared_memory_is_rejected(cuda):
     atol = torch.from_numpy(f["atol"]).cuda()
     with pytest.raises(_abi.FastodeError, match="shared memory"):
         b.step(k, float(f["dt"]), atol, float(f["rtol"]))
+
+
+@pytest.mark.parametrize("kernel", ["compact", "pipelined", "plain"])
+@pytest.mark.parametrize("n,R", [(1, 1), (2, 2), (3, 4)])
+def test_tiny_mechanisms_match_the_oracle(cuda, kernel, n, R):
+    """One, two and three species: the compact kernel's halves are empty or a
+    single row; every kernel gives the oracle's Counts and states."""
+    from fastode_gb300 import Algorithm
+    from fastode_gb300 import synthetic as syn
+    from fastode_gb300.batch import Batch
+    torch = cuda
+    sm = syn.synthetic_mechanism(n, R, seed=3)
+    wl = syn.Workload("tiny", sm, syn.synthetic_cells(sm, 32, seed=4), 30.0, 3, 1e-3, 32, True)
+    ks = [wl.k_at(i) for i in range(wl.intervals)]
+    b = Batch(sm.mech, wl.cells.Y0, group_size=32, algorithm=Algorithm(kernel=kernel))
+    atol = torch.from_numpy(wl.atol).cuda()
+    for i in range(wl.intervals):
+        b.step(torch.from_numpy(np.ascontiguousarray(ks[i].T)).cuda(), wl.dt, atol, wl.rtol)
+    Yo, co, so, _, _ = _oracle(sm.mech, wl.cells.Y0, ks, wl.dt, wl.atol, wl.rtol, 32, wl.intervals)
+    assert tuple(b.counts.cpu().numpy()[0]) == co[0].as_tuple()
+    assert b.statuses() == [so[0][-1]]
+    assert rel_err(b.state(), Yo).max() <= 1e-10

@@ -247,7 +247,7 @@ def compact_emulator(tmp_path_factory):
     return out
 
 
-@pytest.mark.parametrize("which", ["ros3_20x40", "ros3_210x500", "ts1", "dae", "60x40", "120x260"])
+@pytest.mark.parametrize("which", ["ros3_20x40", "ros3_210x500", "ts1", "dae", "60x40", "120x260", "1x1", "2x2", "3x4"])
 def test_compact_tables_reproduce_the_plain_factorization(compact_emulator, tmp_path, which):
     """The compact variant's two-pass elimination stream and split solves,
     executed on the host over the tables the library builds, give the plain
@@ -261,6 +261,9 @@ def test_compact_tables_reproduce_the_plain_factorization(compact_emulator, tmp_
         mech = table_mechanism(load("ts1_tier1_30s"))
     elif which == "dae":
         mech = syn.dae_constrained(n_cells=32, intervals=1).sm.mech
+    elif which in ("1x1", "2x2", "3x4"):                 # empty and one-row halves
+        n, r = (int(v) for v in which.split("x"))
+        mech = syn.synthetic_mechanism(n, r, seed=1).mech
     else:
         mech = {"60x40": syn.batched_uneven(n_cells=96, intervals=1)[0],
                 "120x260": syn.batched_uneven(n_cells=96, intervals=1)[1]}[which].sm.mech
