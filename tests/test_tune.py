@@ -38,3 +38,21 @@ def test_autotune_skips_configs_that_do_not_fit():
 def test_autotune_raises_when_nothing_fits():
     with pytest.raises(ValueError):
         autotune(lambda c: 1.0, 5000, [Config("pipelined", 64)])
+
+
+def test_per_kernel_shared_memory():
+    """With one figure per kernel, a group size that only the compact
+    kernel's half rows fit is measured for compact and skipped for the
+    others (210 species, 256 lanes: 105 doubles per cell fit, 210 do not)."""
+    smem = {"compact": 105, "pipelined": 210, "plain": 210}
+    assert fits(smem, 256, "compact") and not fits(smem, 256, "pipelined")
+    measured = []
+
+    def measure(c):
+        measured.append(c)
+        return 1.0
+
+    r = autotune(measure, smem, candidates(smem, group_sizes=(256,), persistent=(False,)))
+    assert measured == [Config("compact", 256, False)]
+    assert r.best == Config("compact", 256, False)
+    assert [c.kernel for c, v in r.table if v is None] == ["pipelined", "plain"]
