@@ -117,6 +117,24 @@ class HostState:
         self.status_out = torch.empty(self.ngroups, dtype=torch.int32).pin_memory()
         self.opts = self.alg.options()
         self.shape = (C_cells, n, R)
+        self._overlap = None
+
+    def overlap_buffers(self):
+        """The second stream and the extra buffers of ``solve_host_intervals``
+        (a second rate-constant buffer, two staging states, a second pinned
+        output), made on first use and kept."""
+        import torch
+        if self._overlap is None:
+            dev = self.Y.device
+            self._overlap = {
+                "side": torch.cuda.Stream(dev),
+                "kbuf": [self.k, torch.empty_like(self.k)],
+                "stage": [torch.empty_like(self.Y) for _ in range(2)],
+                "stage_st": [torch.empty_like(self.status) for _ in range(2)],
+                "yout": [self.Y_out, torch.empty(self.Y_out.shape, dtype=torch.float64).pin_memory()],
+                "stout": [self.status_out, torch.empty(self.status_out.shape, dtype=torch.int32).pin_memory()],
+            }
+        return self._overlap
 
 
 def solve_host(mech, Y, k, dt, atol, rtol, state: HostState = None, group_size: int = 32,
@@ -154,3 +172,88 @@ def solve_host(mech, Y, k, dt, atol, rtol, state: HostState = None, group_size: 
     h2d = Yt.numel() * 8 + kt.numel() * 8 + n * 8
     d2h = state.Y_out.numel() * 8 + state.status_out.numel() * 4
     return state.Y_out, state, (h2d, d2h)
+
+
+def solve_host_intervals(mech, Y, ks, dt, atol, rtol, state: HostState = None, group_size: int = 32,
+                         algorithm: Algorithm = None, mass=None, slots: int = 0, on_result=None):
+    """``solve_host`` over several intervals with the copies overlapped: Y
+    (C, n) is the host state at the start and ks a sequence of host (C, R)
+    rate-constant arrays, one per interval. The state stays on the device
+    between intervals; each interval's rate constants are copied in on a
+    second stream while the previous interval integrates, and each
+    interval's state and statuses are copied out on that stream while the
+    next one integrates. on_result(i, Y_host, status_host), when given, is
+    called with every interval's result as soon as it is on the host; both
+    tensors are pinned buffers that are overwritten two intervals later (copy
+    them to keep them). Returns (the last interval's Y as a host tensor,
+    state, (bytes host-to-device, bytes device-to-host))."""
+    import torch
+    ks = list(ks)
+    if not ks:
+        raise ValueError("no intervals")
+
+    def host(a):
+        return a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64))
+
+    Yt = host(Y)
+    C_cells, n = Yt.shape
+    R = host(ks[0]).shape[1]
+    if state is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+        state = HostState(mech, C_cells, n, R, group_size, algorithm, mass, slots, dev)
+    if state.shape != (C_cells, n, R):
+        raise ValueError("state was made for other shapes")
+    dev = state.Y.device
+    comp = torch.cuda.current_stream(dev)
+    ob = state.overlap_buffers()
+    side, kbuf, stage, stage_st, yout, stout = (ob[k] for k in ("side", "kbuf", "stage", "stage_st", "yout", "stout"))
+    side.wait_stream(comp)                        # the buffers' last users were on the compute stream
+    at = torch.from_numpy(np.array(np.broadcast_to(np.asarray(atol, dtype=np.float64), (n,))))
+    state.atol.copy_(at, non_blocking=False)
+    state.Y.copy_(Yt, non_blocking=True)
+    kbuf[0].copy_(host(ks[0]), non_blocking=True)
+    k_ready = [None, None]
+    solved = [None] * len(ks)
+    copied = [None] * len(ks)
+    h2d = Yt.numel() * 8 + n * 8 + host(ks[0]).numel() * 8
+    d2h = 0
+
+    def deliver(j):
+        copied[j].synchronize()
+        if on_result is not None:
+            on_result(j, yout[j % 2], stout[j % 2])
+
+    for i in range(len(ks)):
+        if i + 1 < len(ks):                       # rate constants of the next interval
+            kn = host(ks[i + 1])
+            with torch.cuda.stream(side):
+                if i >= 1:
+                    side.wait_event(solved[i - 1])   # its buffer was interval i-1's
+                kbuf[(i + 1) % 2].copy_(kn, non_blocking=True)
+                k_ready[(i + 1) % 2] = side.record_event()
+            h2d += kn.numel() * 8
+        if i >= 1:
+            comp.wait_event(k_ready[i % 2])
+        kb = kbuf[i % 2]
+        rc = _abi.lib().fo_solve(
+            state.plan.handle, C.byref(state.opts), state.ngroups, state.offsets.data_ptr(), state.max_cells,
+            state.Y.data_ptr(), n, 1, kb.data_ptr(), R, 1, state.atol.data_ptr(), float(rtol), float(dt),
+            state.memory.data_ptr(), state.counts.data_ptr(), state.status.data_ptr(),
+            state.ws.data_ptr(), state.ws.numel(), state.slots, None, 0, None, C.c_void_p(comp.cuda_stream))
+        _abi.check(rc, "fo_solve")
+        if i >= 2:
+            comp.wait_event(copied[i - 2])        # the staging buffers' previous copy-out
+        stage[i % 2].copy_(state.Y)
+        stage_st[i % 2].copy_(state.status)
+        solved[i] = comp.record_event()
+        with torch.cuda.stream(side):
+            side.wait_event(solved[i])
+            yout[i % 2].copy_(stage[i % 2], non_blocking=True)
+            stout[i % 2].copy_(stage_st[i % 2], non_blocking=True)
+            copied[i] = side.record_event()
+        d2h += yout[i % 2].numel() * 8 + stout[i % 2].numel() * 4
+        if i >= 1:
+            deliver(i - 1)
+    deliver(len(ks) - 1)
+    comp.wait_stream(side)
+    return yout[(len(ks) - 1) % 2], state, (h2d, d2h)
