@@ -301,7 +301,10 @@ std::vector<int> refine_order(const fo_mechanism_desc& m, const std::vector<int>
   if (n < 3) return start;
   FmaCounter counter(m);
   const int64_t kWorkBudget = 600000000;
-  const int64_t moves = std::max<int64_t>(1000, std::min<int64_t>(20000, kWorkBudget / std::max<int64_t>(1, counter.work(start))));
+  // the operation budget bounds the host time for large mechanisms; below a
+  // few hundred moves the search would not get anywhere, so it is skipped
+  const int64_t moves = std::min<int64_t>(20000, kWorkBudget / std::max<int64_t>(1, counter.work(start)));
+  if (moves < 200) return start;
   std::vector<int> order = start, best = start, trial(n);
   int64_t cur = counter.count(start, INT64_MAX), best_cost = cur;
   const int64_t start_cost = cur;
