@@ -269,7 +269,6 @@ def run_ours(args, rank, world):
         pinned_k = [torch.from_numpy(wl.k_at(i)).pin_memory() for i in range(e2e_steps)]
         Y0h = torch.from_numpy(cells.Y0.copy()).pin_memory()
         alg = Algorithm(kernel=args.kernel, ordering=args.ordering)
-        resident = Cc * e2e_steps / (sum(interval_ms[:e2e_steps]) / 1e3)
         # (1) the overlapped host API: the state stays on the device, every
         # interval's rate constants go in and its state and statuses come out,
         # on a second stream while the device integrates
@@ -294,13 +293,17 @@ def run_ours(args, rank, world):
             h2d1 += moved[0]
             d2h1 += moved[1]
         call_s = time.perf_counter() - t0
-        e2e = {"value": Cc * e2e_steps / e2e_s, "unit": "cell-intervals/s", "steps": e2e_steps,
+        # whole job: every rank runs the same intervals; the slowest rank's time
+        e2e_s = max_over_ranks(e2e_s, world, dev)
+        call_s = max_over_ranks(call_s, world, dev)
+        resident = job_value(Cc * e2e_steps, world, max_over_ranks(sum(interval_ms[:e2e_steps]) / 1e3, world, dev))
+        e2e = {"value": job_value(Cc * e2e_steps, world, e2e_s), "unit": "cell-intervals/s", "steps": e2e_steps,
                "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
                "device_resident_same_intervals": resident,
                "api": "fastode_gb300.batch.solve_host_intervals (host (C,n) state in once, host (C,R) rate "
                       "constants in and the (C,n) state and statuses out every interval, copies overlapped "
                       "with the integration; the first intervals of the job from the initial state)",
-               "per_call": {"value": Cc * e2e_steps / call_s, "unit": "cell-intervals/s",
+               "per_call": {"value": job_value(Cc * e2e_steps, world, call_s), "unit": "cell-intervals/s",
                             "h2d_bytes_per_step": h2d1 // e2e_steps, "d2h_bytes_per_step": d2h1 // e2e_steps,
                             "api": "fastode_gb300.batch.solve_host, one call per interval (state in and out "
                                    "every call)"}}
