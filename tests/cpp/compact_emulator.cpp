@@ -40,6 +40,28 @@ int main(int argc, char** argv) {
     printf("tables: %s\n", err.c_str());
     return 1;
   }
+  // Both packed elimination streams must be hazard-free within each chunk
+  // (the device reads a chunk's work-row values before running it): no slot is
+  // updated twice in a chunk, and no multiplier reads a slot an earlier update
+  // of its chunk wrote. Rows (pipelined) and passes (compact) start on chunks.
+  auto hazard_free = [](const std::vector<uint32_t>& st, const std::vector<int32_t>& ptr, uint32_t special) {
+    for (int32_t p : ptr)
+      if (p % fo::kStreamChunk) return false;
+    for (size_t c0 = 0; c0 < st.size(); c0 += fo::kStreamChunk) {
+      std::vector<uint32_t> updated;
+      for (size_t w = c0; w < c0 + fo::kStreamChunk && w < st.size(); ++w) {
+        const uint32_t word = st[w], y = word & 0x7fffu;
+        if (!(word & 0x8000u) && y >= special) continue;        // padding or reload
+        for (uint32_t u : updated)
+          if (u == y) return false;
+        if (!(word & 0x8000u)) updated.push_back(y);
+      }
+    }
+    return true;
+  };
+  std::vector<int32_t> el_starts(t.el_ptr.begin(), t.el_ptr.end());
+  if (!t.elp.empty() && !hazard_free(t.elp, el_starts, 0x7fffu)) return 17;
+  if (!hazard_free(t.cep, t.ce_ptr, fo::kReloadSlot)) return 18;
   const int n = t.n, nlu = (int)t.lu_col.size(), nj = (int)t.j_col.size();
   std::mt19937_64 rng(7);
   std::uniform_real_distribution<double> U(-1.0, 1.0);
