@@ -156,9 +156,10 @@ typedef struct fo_options {
 #define FO_LOOP_BACKWARD_EULER 2
 
 /* Kernel variants of the factorization and solves. PIPELINED streams the
- * elimination schedule with register double-buffering (the fast path);
- * PLAIN is the direct row-by-row loop, kept as the baseline it is measured
- * against. */
+ * elimination schedule in hazard-free chunks through a shared-memory operand
+ * ring, with the whole compressed row on chip; PLAIN is the direct
+ * row-by-row loop, kept as the baseline it is measured against; COMPACT
+ * (below) is the fastest where its tables fit. */
 #define FO_VARIANT_PIPELINED 0
 #define FO_VARIANT_PLAIN 1
 /* COMPACT eliminates every row in two passes over halves of its slots (the
