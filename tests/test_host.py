@@ -271,3 +271,19 @@ def test_compact_tables_reproduce_the_plain_factorization(compact_emulator, tmp_
     _write_descriptor(desc, mech)
     r = subprocess.run([str(compact_emulator), str(desc)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_large_mechanism_falls_back_from_the_stream_kernels(built_library):
+    """A mechanism whose factor has more than 65,536 entries gets no packed
+    streams: the plan reports the plain kernel's shared memory for the
+    compact kernel too (the launch then runs the plain loops), and the
+    ordering search stays within its operation budget."""
+    import time
+    from fastode_gb300 import synthetic as syn
+    from fastode_gb300.plan import analyze
+    sm = syn.synthetic_mechanism(1000, 2500, seed=5)
+    t0 = time.perf_counter()
+    info = analyze(sm.mech)
+    assert time.perf_counter() - t0 < 30.0
+    assert info["nnz_lu"] > 65536
+    assert info["compact_smem_doubles_per_cell"] == info["smem_doubles_per_cell"]
