@@ -158,6 +158,61 @@ def algorithmic_flops(plan, counts_rows, offsets):
     return float((per_group * cells).sum())
 
 
+SUBSET_FIXTURE = ROOT / "tests" / "golden" / "ros3_210x500_subset.npz"
+
+
+class PlainInputs:
+    """Host inputs of the 210/500 workload: Y0, the (C, R) rate constants at
+    t = 0 and the (intervals, C) diurnal factors, built by the generator
+    (synthetic.rate_constants). When the workload is the full 65,536-cell job,
+    the cells of the parity subset take the reference's own inputs from its
+    fixture (the reference ran on those exact values)."""
+
+    def __init__(self, wl, intervals):
+        from fastode_gb300 import synthetic as syn
+        self.wl = wl
+        self.photo = np.nonzero(wl.sm.photolytic)[0].astype(np.int32)
+        self.J = wl.sm.J[self.photo]
+        self.k0 = wl.k_at(0)
+        self.fac = syn.photolysis_factors(wl.cells, wl.dt, intervals)
+        self.Y0 = wl.cells.Y0.copy()
+        self.subset = None
+        if wl.cells.C == 65536 and SUBSET_FIXTURE.exists():
+            f = dict(np.load(SUBSET_FIXTURE))
+            c = f["cells"]
+            m = min(intervals, int(f["intervals"]))
+            self.k0[c] = f["k0"]
+            self.fac[:m, c] = f["f"][:m]
+            self.Y0[c] = f["Y0"]
+            self.subset = f
+
+    def k_at(self, i):
+        """(C, R) rate constants of interval i, as the device builds them."""
+        k = self.k0.copy()
+        k[:, self.photo] = self.J[None, :] * self.fac[i][:, None]
+        return k
+
+    def parity(self, counts, status, Y, intervals):
+        """The measured run against the reference on the parity subset after
+        `intervals` intervals from the initial state."""
+        f = self.subset
+        if f is None or intervals > int(f["intervals"]):
+            return None
+        groups = np.asarray(f["groups"])
+        gs = int(f["group_size"])
+        out = {"groups": len(groups), "intervals": intervals,
+               "reference": "tests/golden/ros3_210x500_subset.npz (the reference run on these cells)",
+               "counts_equal": bool(np.array_equal(counts[groups], f["counts"][:, intervals - 1])),
+               "status_equal": bool(np.array_equal(status[groups], f["status"][:, intervals - 1]))}
+        snaps = list(np.asarray(f["snapshots"]))
+        if intervals in snaps:
+            ref = f["Y_snap"][snaps.index(intervals)]
+            got = Y[np.asarray(f["cells"])]
+            out["state_max_rel"] = float((np.abs(got - ref) / np.maximum(np.abs(ref), 1e-14)).max())
+            out["state_rtol"] = 1e-10
+        return out
+
+
 def run_ours(args, rank, world):
     import ctypes as C
     import torch
@@ -174,28 +229,25 @@ def run_ours(args, rank, world):
     wl = syn.plain_large(n_cells=args.cells, intervals=args.steps)
     sm, cells = wl.sm, wl.cells
     Cc, R, n = cells.C, sm.R, sm.n
-    M = cells.p / (syn.R_GAS * cells.T)
-    photo = np.nonzero(sm.photolytic)[0].astype(np.int32)
+    # Inputs as the reference builds them (synthetic.rate_constants on the
+    # host: k at t = 0 and every interval's diurnal factors), uploaded once;
+    # on the parity subset the reference's own inputs, read from its fixture.
+    # Per interval the device sets the photolysis columns to J * f (one IEEE
+    # product, fo_photolysis_factor), so the device integrates exactly k_at(i).
+    inputs = PlainInputs(wl, max(args.steps, args.warmup, args.e2e_steps))
+    photo = inputs.photo
     d = {name: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for name, v in
-         dict(A=sm.A, E=sm.E, power=sm.mech.third_body_power, T=cells.T, M=M, phase=cells.phase,
-              J=sm.J[photo], rxn=photo, atol=wl.atol).items()}
-    k = torch.empty((R, Cc), dtype=torch.float64, device=dev)          # cells fastest
+         dict(J=inputs.J, rxn=photo, atol=wl.atol, fac=inputs.fac).items()}
+    k = torch.from_numpy(np.ascontiguousarray(inputs.k0.T)).to(dev)          # (R, C), cells fastest
     stream = torch.cuda.current_stream(dev)
     sp = C.c_void_p(stream.cuda_stream)
-    omega = 2.0 * np.pi / 86400.0
-
-    def thermal():
-        _abi.check(lib.fo_rate_constants(Cc, R, d["A"].data_ptr(), d["E"].data_ptr(), d["power"].data_ptr(),
-                                         d["T"].data_ptr(), d["M"].data_ptr(), k.data_ptr(), 1, Cc, sp),
-                   "fo_rate_constants")
 
     def photolysis(i):
-        _abi.check(lib.fo_update_photolysis(Cc, len(photo), d["rxn"].data_ptr(), d["J"].data_ptr(),
-                                            d["phase"].data_ptr(), omega, i * wl.dt, k.data_ptr(), 1, Cc, sp),
-                   "fo_update_photolysis")
+        _abi.check(lib.fo_photolysis_factor(Cc, len(photo), d["rxn"].data_ptr(), d["J"].data_ptr(),
+                                            d["fac"][i].data_ptr(), k.data_ptr(), 1, Cc, sp),
+                   "fo_photolysis_factor")
 
-    thermal()
-    Y0 = torch.from_numpy(cells.Y0).to(dev)
+    Y0 = torch.from_numpy(inputs.Y0).to(dev)
     from fastode_gb300 import Algorithm
     batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel=args.kernel, ordering=args.ordering))
 
@@ -216,6 +268,8 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     marks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    n_plain = min(args.plain_steps, args.steps)
+    counts_at_plain = torch.empty_like(batch.counts)
     with Clocks(dev.index) as clocks:
         start.record()
         for i in range(args.steps):
@@ -224,6 +278,8 @@ def run_ours(args, rank, world):
             ev[i][0].record()
             batch.step(k, wl.dt, d["atol"], wl.rtol)
             ev[i][1].record()
+            if i + 1 == n_plain:
+                counts_at_plain.copy_(batch.counts, non_blocking=True)   # 213 KB, device to device
         end.record()
         torch.cuda.synchronize()
     elapsed = start.elapsed_time(end) / 1e3
@@ -232,7 +288,6 @@ def run_ours(args, rank, world):
     # the plain one-group-per-block kernel (FO_VARIANT_PLAIN) on the first
     # intervals of the same job, for the "vs plain GPU" comparison
     plain = None
-    n_plain = min(args.plain_steps, args.steps)
     if n_plain > 0 and args.kernel != "plain":
         pb = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel="plain", ordering=args.ordering))
         torch.cuda.synchronize()
@@ -247,9 +302,8 @@ def run_ours(args, rank, world):
         ours_s = sum(interval_ms[:n_plain]) / 1e3
         plain = {"value": Cc * n_plain / plain_s, "unit": "cell-intervals/s", "intervals": n_plain,
                  "ours_same_intervals": Cc * n_plain / ours_s, "speedup": plain_s / ours_s,
-                 "same_counts": bool(np.array_equal(pb.counts.cpu().numpy().sum(0),
-                                                    batch.counts.cpu().numpy().sum(0))) if n_plain == args.steps
-                 else None}
+                 "same_counts": bool(np.array_equal(pb.counts.cpu().numpy(), counts_at_plain.cpu().numpy())),
+                 "same_counts_scope": f"Counts of every group after the first {n_plain} intervals"}
         del pb
     elapsed = max_over_ranks(elapsed, world, dev)
     solve_ms = [a.elapsed_time(b) for a, b in ev]
@@ -266,8 +320,8 @@ def run_ours(args, rank, world):
     e2e = None
     if e2e_steps > 0:
         from fastode_gb300.batch import HostState, solve_host_intervals
-        pinned_k = [torch.from_numpy(wl.k_at(i)).pin_memory() for i in range(e2e_steps)]
-        Y0h = torch.from_numpy(cells.Y0.copy()).pin_memory()
+        pinned_k = [torch.from_numpy(inputs.k_at(i)).pin_memory() for i in range(e2e_steps)]
+        Y0h = torch.from_numpy(inputs.Y0.copy()).pin_memory()
         alg = Algorithm(kernel=args.kernel, ordering=args.ordering)
         # (1) the overlapped host API: the state stays on the device, every
         # interval's rate constants go in and its state and statuses come out,
@@ -337,7 +391,9 @@ def run_ours(args, rank, world):
         "e2e": e2e,
         "plain_gpu": plain,
         "kernel_variant": args.kernel,
+        "generated_module": batch.plan.gen_info,
         "lu": {k: batch.plan.info[k] for k in ("ordering", "lu_fma", "nnz_lu", "solve_fma")},
+        "parity": inputs.parity(counts, batch.status.cpu().numpy(), batch.state(), args.steps),
         "interval_ms": {"first": interval_ms[0], "median": float(np.median(interval_ms)),
                         "max": float(max(interval_ms))},
     }
@@ -643,7 +699,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--cells", type=int, default=65536)
     ap.add_argument("--slots", type=int, default=0)
-    ap.add_argument("--kernel", default="compact", choices=["compact", "pipelined", "plain"])
+    ap.add_argument("--kernel", default="generated", choices=["generated", "compact", "pipelined", "plain"],
+                    help="generated: the mechanism's own factorization and solves as straight-line code "
+                         "(compiled when the plan is made, outside the timed region); the others are "
+                         "table-driven")
     ap.add_argument("--ordering", default="auto", choices=["auto", "refined", "min_fill", "min_degree", "natural"],
                     help="elimination order of the sparse LU (auto: the greedy orders refined by local search)")
     ap.add_argument("--plain-steps", type=int, default=10)

@@ -54,9 +54,18 @@ class Options(C.Structure):
                 ("reductions", C.c_double * 8), ("small", C.c_double)]
 
 
-VARIANTS = {"pipelined": 0, "plain": 1, "compact": 2}
+VARIANTS = {"pipelined": 0, "plain": 1, "compact": 2, "generated": 3}
 LOOPS = {"algorithm": 0, "restarting": 1, "backward-euler": 2}
 SCORE_RULES = {"ts1": 0, "digits": 1}
+
+
+class GenInfo(C.Structure):
+    _fields_ = [("from_cache", C.c_int32), ("registers", C.c_int32), ("tile", C.c_int32),
+                ("local_bytes", C.c_int32), ("seconds", C.c_double), ("ptx_bytes", C.c_int64),
+                ("cubin_bytes", C.c_int64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 class BatchDesc(C.Structure):
@@ -82,6 +91,8 @@ SIGNATURES = {
     "fo_plan_destroy": (C.c_int, [_P]),
     "fo_plan_permutation": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "fo_workspace_bytes": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_size_t)]),
+    "fo_plan_generate": (C.c_int, [_P, C.c_char_p, C.POINTER(GenInfo)]),
+    "fo_generate_check": (C.c_int, [C.POINTER(MechanismDesc), _I32, _I32, C.POINTER(GenInfo)]),
     "fo_solve": (C.c_int, [_P, C.POINTER(Options), _I32, _P, _I32,
                            _P, _I64, _I64, _P, _I64, _I64, _P, _D, _D,
                            _P, _P, _P, _P, C.c_size_t, _I32, _P, _I32, _P, _P]),
@@ -91,6 +102,7 @@ SIGNATURES = {
     "fo_eval_jac": (C.c_int, [_P, _I32, _P, _I64, _I64, _P, _I64, _I64, _P, _P]),
     "fo_rate_constants": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
     "fo_update_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _D, _P, _I64, _I64, _P]),
+    "fo_photolysis_factor": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _I64, _I64, _P]),
     "fo_fp64_fma_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "fo_scale_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _P, _I64, _I64, _P]),
     "fo_score_accumulate": (C.c_int, [_I32, _I32, _P, _I64, _I64, _I32, _P, _P, _I64, _I64, _D, _I32,

@@ -55,7 +55,7 @@ class Batch:
         if self.trace_cap > 0:
             self.trace = torch.zeros((self.ngroups, self.trace_cap, 4), dtype=torch.float64, device=dev)
             self.trace_len = torch.zeros(self.ngroups, dtype=torch.int32, device=dev)
-        self.opts = self.alg.options()
+        self.opts = self.plan.options_for(self.alg, self.max_cells)
         self.stream = stream
 
     def _stream(self):
@@ -115,7 +115,7 @@ class HostState:
         self.ws = torch.empty(self.plan.workspace_bytes(grid, self.max_cells), dtype=torch.uint8, device=dev)
         self.Y_out = torch.empty((C_cells, n), dtype=torch.float64).pin_memory()
         self.status_out = torch.empty(self.ngroups, dtype=torch.int32).pin_memory()
-        self.opts = self.alg.options()
+        self.opts = self.plan.options_for(self.alg, self.max_cells)
         self.shape = (C_cells, n, R)
         self._overlap = None
 

@@ -19,7 +19,13 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libfastode_gb300.so"
-SOURCES = ["integrator.cu", "adjoint.cu", "abi.cu", "utility.cu", "scoring.cu", "static_scratch.cu", "symbolic.cpp"]
+SOURCES = ["integrator.cu", "adjoint.cu", "abi.cu", "utility.cu", "scoring.cu", "static_scratch.cu", "symbolic.cpp",
+           "codegen.cpp", "jit.cpp", "embed.cpp"]
+# the integrator of the generated variant, compiled as relocatable device code
+# and embedded in the library (embed.cpp), where each plan links it with its
+# mechanism's generated code
+RDC_SOURCE = "generated.cu"
+RDC_NAME = "generated_rdc.cubin"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,7 +44,7 @@ def _stale(target: Path) -> bool:
     if not target.exists():
         return True
     t = target.stat().st_mtime
-    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
+    deps = [CSRC / s for s in SOURCES + [RDC_SOURCE]] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
     deps.append(ROOT / "include" / "fastode_gb300.h")
     return any(d.stat().st_mtime > t for d in deps if d.exists())
 
@@ -49,16 +55,26 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         return target
     LIBDIR.mkdir(exist_ok=True)
     tmp = target.with_suffix(".so.tmp%d" % os.getpid())
-    cmd = [nvcc_path(), "-shared", "-Xcompiler", "-fPIC", *ARCH, "-O3", "-lineinfo", "-std=c++17",
-           "--threads", "0", f"-I{ROOT / 'include'}", *[str(CSRC / s) for s in SOURCES], "-o", str(tmp)]
-    if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-        print(" ".join(cmd), file=sys.stderr)
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + r.stdout + r.stderr)
-    if verbose:
-        print(r.stdout + r.stderr, file=sys.stderr)
+    rdc = LIBDIR / RDC_NAME
+    rdc_tmp = rdc.with_suffix(".cubin.tmp%d" % os.getpid())
+    steps = [
+        [nvcc_path(), "-cubin", "-rdc=true", *ARCH, "-O3", "-lineinfo", "-std=c++17", f"-I{ROOT / 'include'}",
+         str(CSRC / RDC_SOURCE), "-o", str(rdc_tmp)],
+        [nvcc_path(), "-shared", "-Xcompiler", "-fPIC", *ARCH, "-O3", "-lineinfo", "-std=c++17",
+         "--threads", "0", f"-I{ROOT / 'include'}", f'-DFO_GENERATED_RDC="{rdc}"',
+         *[str(CSRC / s) for s in SOURCES], "-ldl", "-o", str(tmp)],
+    ]
+    for i, cmd in enumerate(steps):
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed:\n" + r.stdout + r.stderr)
+        if verbose:
+            print(r.stdout + r.stderr, file=sys.stderr)
+        if i == 0:
+            os.replace(rdc_tmp, rdc)
     os.replace(tmp, target)
     return target
 

@@ -7,12 +7,15 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "device.cuh"
 #include "fastode_gb300.h"
+#include "jit.h"
+#include "layout.h"
 #include "symbolic.h"
 
 namespace fo {
@@ -30,6 +33,9 @@ struct fo_plan {
   fo::DevTables dev;
   void* blob = nullptr;  // device copy of every table
   int device = -1;
+  fo::GenModule* gen = nullptr;  // the generated variant's module (fo_plan_generate)
+  fo_gen_info gen_info{};
+  std::mutex gen_mutex;
 };
 
 namespace {
@@ -53,6 +59,8 @@ int fo::set_last_error(int code, const char* what) { return fail(code, what); }
 
 namespace {
 
+using fo::layout_of;
+
 const fo::DevTableau kTableaus[2] = {
     // ROS3 (fastode/tableaus.py:70-80)
     {0.43586652150845899941601945119356,
@@ -74,23 +82,6 @@ const fo::DevTableau kTableaus[2] = {
      {0.0, 0.0, 0.0, 1.0},
      {1, 0, 1, 1}},
 };
-
-fo::ScratchLayout layout_of(const fo::HostTables& t) {
-  fo::ScratchLayout s;
-  int64_t o = 0;
-  s.lu = o; o += (int64_t)t.lu_col.size();
-  s.negj = o; o += (int64_t)t.j_col.size();
-  s.d = o; o += (int64_t)t.R * t.P;
-  s.r = o; o += t.R;
-  s.y = o; o += t.n;
-  s.ynew = o; o += t.n;
-  s.f0 = o; o += t.n;
-  s.ft = o; o += t.n;
-  s.yr = o; o += t.n;
-  s.k = o; o += 4LL * t.n;
-  s.items = o;
-  return s;
-}
 
 int lanes_for(int cells) { return ((cells + 31) / 32) * 32; }
 
@@ -168,6 +159,20 @@ int fo_analyze(const fo_mechanism_desc* mech, int32_t ordering, fo_plan_info* in
     if (!err.empty()) return fail(FO_E_INVALID, err);
     fill_info(t, info);
     if (perm) std::memcpy(perm, t.perm.data(), sizeof(int32_t) * t.n);
+  } catch (const std::bad_alloc&) {
+    return fail(FO_E_ALLOC, "host allocation failed");
+  }
+  return FO_OK;
+}
+
+int fo_generate_check(const fo_mechanism_desc* mech, int32_t ordering, int32_t link, fo_gen_info* info) {
+  if (!mech) return fail(FO_E_INVALID, "null argument");
+  try {
+    fo::HostTables t;
+    std::string err = fo::build_tables(*mech, ordering, &t);
+    if (!err.empty()) return fail(FO_E_INVALID, err);
+    int rc = fo::gen_check(t, link != 0, info, &err);
+    if (rc != FO_OK) return fail(rc, err);
   } catch (const std::bad_alloc&) {
     return fail(FO_E_ALLOC, "host allocation failed");
   }
@@ -282,6 +287,7 @@ int fo_plan_info_get(const fo_plan* plan, fo_plan_info* info) {
 
 int fo_plan_destroy(fo_plan* plan) {
   if (!plan) return FO_OK;
+  fo::gen_destroy(plan->gen);
   if (plan->blob) cudaFree(plan->blob);
   delete plan;
   return FO_OK;
@@ -290,6 +296,20 @@ int fo_plan_destroy(fo_plan* plan) {
 int fo_plan_permutation(const fo_plan* plan, int32_t* perm) {
   if (!plan || !perm) return fail(FO_E_INVALID, "null argument");
   std::memcpy(perm, plan->host.perm.data(), sizeof(int32_t) * plan->host.n);
+  return FO_OK;
+}
+
+int fo_plan_generate(fo_plan* plan, const char* cache_dir, fo_gen_info* info) {
+  if (!plan) return fail(FO_E_INVALID, "null plan");
+  std::lock_guard<std::mutex> lock(plan->gen_mutex);
+  if (!plan->gen) {
+    std::string err;
+    fo_gen_info gi;
+    int rc = fo::gen_create(plan->host, cache_dir, &plan->gen, &gi, &err);
+    if (rc != FO_OK) return fail(rc, err);
+    plan->gen_info = gi;
+  }
+  if (info) *info = plan->gen_info;
   return FO_OK;
 }
 
@@ -314,9 +334,15 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
     return fail(FO_E_INVALID, "null argument");
   if (opt->tableau != FO_TABLEAU_ROS3 && opt->tableau != FO_TABLEAU_RODAS3)
     return fail(FO_E_INVALID, "unknown tableau");
-  if (opt->variant != FO_VARIANT_PIPELINED && opt->variant != FO_VARIANT_PLAIN && opt->variant != FO_VARIANT_COMPACT)
+  if (opt->variant != FO_VARIANT_PIPELINED && opt->variant != FO_VARIANT_PLAIN && opt->variant != FO_VARIANT_COMPACT &&
+      opt->variant != FO_VARIANT_GENERATED)
     return fail(FO_E_INVALID, "unknown kernel variant");
   int variant = opt->variant;
+  if (variant == FO_VARIANT_GENERATED) {
+    if (!plan->gen) return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED needs fo_plan_generate on this plan first");
+    if (max_group_cells <= 0 || max_group_cells > 32)
+      return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED runs groups of at most 32 cells");
+  }
   if (variant == FO_VARIANT_COMPACT && plan->dev.cep == nullptr) variant = FO_VARIANT_PIPELINED;
   if (variant == FO_VARIANT_PIPELINED && plan->dev.elp == nullptr) variant = FO_VARIANT_PLAIN;
   if (max_group_cells <= 0 || max_group_cells > kMaxLanes)
@@ -324,7 +350,11 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
   if (!(dt > 0.0)) return fail(FO_E_INVALID, "dt must be positive");
   if (opt->max_steps < 0) return fail(FO_E_INVALID, "max_steps must be non-negative");
   const int lanes = lanes_for(max_group_cells);
-  const size_t smem = smem_bytes(plan->host, lanes, variant);
+  // the generated variant keeps nothing on chip but the reduction buffer,
+  // plus the projection's dense work row for a constrained mechanism
+  const size_t smem = variant == FO_VARIANT_GENERATED
+                          ? sizeof(double) * (32 + (plan->dev.has_constraints ? (size_t)plan->host.n * lanes : 0))
+                          : smem_bytes(plan->host, lanes, variant);
   int dev = 0, smem_max = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
@@ -455,7 +485,8 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   } else {
     p.queue = nullptr;
   }
-  e = fo::launch_solve(p, grid, smem, s);
+  if (p.o.variant == FO_VARIANT_GENERATED) e = fo::gen_launch(plan->gen, p, grid, smem, s);
+  else e = fo::launch_solve(p, grid, smem, s);
   if (e != cudaSuccess) return cuda_fail(e, "solve kernel launch");
   return FO_OK;
 }
@@ -493,6 +524,8 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
                      d.y_species_stride, d.k, d.k_cell_stride, d.k_reaction_stride, d.atol, d.rtol, d.dt, d.memory,
                      d.counts, d.status, &params[j], &sm);
     if (rc != FO_OK) return rc;
+    if (params[j].o.variant == FO_VARIANT_GENERATED)
+      return fail(FO_E_UNSUPPORTED, "the several-mechanism launch runs the table-driven variants");
     smem = std::max(smem, smem_bytes(d.plan->host, L.lanes, params[j].o.variant));
     starts[j + 1] = starts[j] + d.ngroups;
   }
@@ -602,7 +635,8 @@ int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngro
   fo_adjoint_workspace_bytes(plan, ngroups, max_group_cells, max_steps, &need);
   if (workspace_bytes < need) return fail(FO_E_WORKSPACE, "workspace too small");
   a.al = adjoint_layout(plan->host, max_steps);
-  if (a.p.o.variant == FO_VARIANT_COMPACT) {     // the transposed solves need the whole vector on chip
+  if (a.p.o.variant == FO_VARIANT_COMPACT || a.p.o.variant == FO_VARIANT_GENERATED) {
+    // the transposed solves need the whole vector on chip
     a.p.o.variant = plan->dev.elp ? FO_VARIANT_PIPELINED : FO_VARIANT_PLAIN;
     smem = smem_bytes(plan->host, a.p.lanes, a.p.o.variant);
   }

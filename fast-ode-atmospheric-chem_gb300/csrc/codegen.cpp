@@ -1,0 +1,329 @@
+// Straight-line PTX for one mechanism's factorization and triangular solves.
+//
+// Why straight-line code. The table-driven kernels (rosenbrock.cuh) spend
+// about 40 integer, address and control instructions around every FP64
+// multiply-add decoding their streams. Here the pattern is known when the plan
+// is made, so every operand is an immediate offset from one base register and
+// the instruction stream is the arithmetic itself: one DFMA per update plus
+// its share of the operand loads.
+//
+// The factorization: row blocks of `tile` rows, each cut into column tiles of
+// `tile` columns, processed left to right (L tiles, the diagonal tile, U
+// tiles). A tile's entries live in registers from assembly to store; every
+// pivot k that updates the tile contributes the outer product of its
+// multipliers l(i, k) (rows of the tile) and its U row u(k, j) (columns of
+// the tile), loaded once per tile: 2t loads for up to t^2 independent FMAs.
+// Pivots inside the tile follow in ascending order. Each entry therefore
+// receives exactly the updates of the row-by-row elimination, in ascending
+// pivot order, with the same operations (fma(-l, u, a); l = a * (1 / pivot);
+// 1 / pivot by an IEEE division), so the factors are those of every other
+// variant bit for bit. Only structurally nonzero products are emitted: the
+// fill pattern's closure (l(i,k) != 0 and u(k,j) != 0 imply (i,j) in the
+// pattern) makes each pivot's contribution to a tile a full rectangle.
+//
+// The solves: blocks of `solve_block` rows; each row sums its terms in
+// ascending column order, as the plain variant's loops do, so results match
+// that variant bit for bit; a solution value used by several rows of a block
+// is loaded once for the block.
+#include "codegen.h"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+#include "layout.h"
+
+namespace fo {
+namespace {
+
+class Ptx {
+ public:
+  std::string body;
+  int next = 1;  // %d0 is alpha
+
+  int reg() { return next++; }
+
+  void line(const char* fmt, ...) __attribute__((format(printf, 2, 3))) {
+    char buf[160];
+    va_list ap;
+    va_start(ap, fmt);
+    const int len = vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    body.append("\t");
+    body.append(buf, (size_t)std::min<int>(len, (int)sizeof(buf) - 1));
+    body.append("\n");
+  }
+  // value of item `item` of this lane's scratch
+  int load(int64_t item) {
+    const int r = reg();
+    line("ld.global.f64 %%d%d, [%%b+%lld];", r, (long long)(item * 256));
+    return r;
+  }
+  void store(int64_t item, int r) { line("st.global.f64 [%%b+%lld], %%d%d;", (long long)(item * 256), r); }
+  int neg(int x) {
+    const int r = reg();
+    line("neg.f64 %%d%d, %%d%d;", r, x);
+    return r;
+  }
+  int fma(int a, int b, int c) {
+    const int r = reg();
+    line("fma.rn.f64 %%d%d, %%d%d, %%d%d, %%d%d;", r, a, b, c);
+    return r;
+  }
+  int mul(int a, int b) {
+    const int r = reg();
+    line("mul.rn.f64 %%d%d, %%d%d, %%d%d;", r, a, b);
+    return r;
+  }
+  int add(int a, int b) {
+    const int r = reg();
+    line("add.rn.f64 %%d%d, %%d%d, %%d%d;", r, a, b);
+    return r;
+  }
+  int constant(double v) {
+    const int r = reg();
+    unsigned long long bits;
+    static_assert(sizeof(bits) == sizeof(v), "");
+    std::memcpy(&bits, &v, sizeof(v));
+    line("mov.f64 %%d%d, 0d%016llX;", r, bits);
+    return r;
+  }
+  int recip(int x) {
+    const int r = reg();
+    line("div.rn.f64 %%d%d, 0d3FF0000000000000, %%d%d;", r, x);
+    return r;
+  }
+};
+
+// Dense map of the LU storage: position of (i, j), or -1.
+struct Pattern {
+  int n;
+  std::vector<int32_t> pos;
+  int32_t at(int i, int j) const { return pos[(size_t)i * n + j]; }
+};
+
+Pattern pattern_of(const HostTables& t) {
+  Pattern P;
+  P.n = t.n;
+  P.pos.assign((size_t)t.n * t.n, -1);
+  for (int i = 0; i < t.n; ++i)
+    for (int q = t.lu_row_ptr[i]; q < t.lu_row_ptr[i + 1]; ++q) P.pos[(size_t)i * t.n + t.lu_col[q]] = q;
+  return P;
+}
+
+void emit_factor(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pattern& P, int b, int64_t* nfma) {
+  const int n = t.n;
+  // Jacobian entry (assembly order) stored at each LU position, or -1
+  std::vector<int32_t> jac_at(t.lu_col.size(), -1);
+  for (size_t e = 0; e < t.j_lu_pos.size(); ++e) jac_at[t.j_lu_pos[e]] = (int32_t)e;
+  const int nb = (n + b - 1) / b;
+  std::vector<int> a((size_t)b * b);
+  auto A = [&](int i, int j, int i0, int j0) -> int& { return a[(size_t)(i - i0) * b + (j - j0)]; };
+  for (int ib = 0; ib < nb; ++ib) {
+    const int i0 = ib * b, i1 = std::min(n, i0 + b);
+    for (int jb = 0; jb < nb; ++jb) {
+      const int j0 = jb * b, j1 = std::min(n, j0 + b);
+      bool any = false;
+      for (int i = i0; i < i1 && !any; ++i)
+        for (int j = j0; j < j1; ++j)
+          if (P.at(i, j) >= 0) { any = true; break; }
+      if (!any) continue;
+      // assembly: -J (or 0 on fill) plus alpha * mass on the diagonal
+      for (int i = i0; i < i1; ++i)
+        for (int j = j0; j < j1; ++j) {
+          const int q = P.at(i, j);
+          if (q < 0) continue;
+          int v = jac_at[q] >= 0 ? x.load(sl.negj + jac_at[q]) : x.constant(0.0);
+          if (i == j) {
+            const double m = t.mass[i];
+            // alpha * 1 is alpha exactly; any other mass takes the product
+            v = x.add(v, m == 1.0 ? 0 : x.mul(0, x.constant(m)));
+          }
+          A(i, j, i0, j0) = v;
+        }
+      // pivots left of the tile (and above it): outer products
+      const int kmax = std::min(i0, j0);
+      std::vector<int> rows, cols, nl(b), u(b);
+      for (int k = 0; k < kmax; ++k) {
+        rows.clear();
+        cols.clear();
+        for (int i = i0; i < i1; ++i)
+          if (P.at(i, k) >= 0) rows.push_back(i);
+        if (rows.empty()) continue;
+        for (int j = j0; j < j1; ++j)
+          if (P.at(k, j) >= 0) cols.push_back(j);
+        if (cols.empty()) continue;
+        for (int i : rows) nl[i - i0] = x.neg(x.load(sl.lu + P.at(i, k)));
+        for (int j : cols) u[j - j0] = x.load(sl.lu + P.at(k, j));
+        for (int i : rows)
+          for (int j : cols) {
+            if (P.at(i, j) < 0) throw std::logic_error("fill pattern not closed");
+            int& r = A(i, j, i0, j0);
+            r = x.fma(nl[i - i0], u[j - j0], r);
+            ++*nfma;
+          }
+      }
+      if (jb < ib) {
+        // an L tile: the multipliers of pivots j0..j1-1, then their updates
+        // inside the tile
+        for (int k = j0; k < j1; ++k) {
+          rows.clear();
+          for (int i = i0; i < i1; ++i)
+            if (P.at(i, k) >= 0) rows.push_back(i);
+          if (rows.empty()) continue;
+          const int rk = x.load(sl.lu + P.at(k, k));
+          for (int i : rows) {
+            int& l = A(i, k, i0, j0);
+            l = x.mul(l, rk);
+            x.store(sl.lu + P.at(i, k), l);
+            nl[i - i0] = x.neg(l);
+          }
+          for (int j = k + 1; j < j1; ++j) {
+            if (P.at(k, j) < 0) continue;
+            const int uu = x.load(sl.lu + P.at(k, j));
+            for (int i : rows) {
+              int& r = A(i, j, i0, j0);
+              r = x.fma(nl[i - i0], uu, r);
+              ++*nfma;
+            }
+          }
+        }
+      } else if (jb == ib) {
+        // the diagonal tile: dense elimination inside it
+        for (int k = i0; k < i1; ++k) {
+          const int rk = x.recip(A(k, k, i0, j0));
+          x.store(sl.lu + P.at(k, k), rk);
+          for (int j = k + 1; j < i1; ++j)
+            if (P.at(k, j) >= 0) x.store(sl.lu + P.at(k, j), A(k, j, i0, j0));
+          for (int i = k + 1; i < i1; ++i) {
+            if (P.at(i, k) < 0) continue;
+            int& l = A(i, k, i0, j0);
+            l = x.mul(l, rk);
+            x.store(sl.lu + P.at(i, k), l);
+            const int nli = x.neg(l);
+            for (int j = k + 1; j < i1; ++j) {
+              if (P.at(k, j) < 0) continue;
+              int& r = A(i, j, i0, j0);
+              r = x.fma(nli, A(k, j, i0, j0), r);
+              ++*nfma;
+            }
+          }
+        }
+      } else {
+        // a U tile: rows of the block finish in order and update the rows
+        // below them (multipliers from the diagonal tile)
+        for (int k = i0; k < i1; ++k) {
+          cols.clear();
+          for (int j = j0; j < j1; ++j)
+            if (P.at(k, j) >= 0) {
+              cols.push_back(j);
+              x.store(sl.lu + P.at(k, j), A(k, j, i0, j0));
+            }
+          if (cols.empty()) continue;
+          for (int i = k + 1; i < i1; ++i) {
+            if (P.at(i, k) < 0) continue;
+            const int nli = x.neg(x.load(sl.lu + P.at(i, k)));
+            for (int j : cols) {
+              int& r = A(i, j, i0, j0);
+              r = x.fma(nli, A(k, j, i0, j0), r);
+              ++*nfma;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+void emit_solve(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pattern& P, int b) {
+  const int n = t.n;
+  const int nb = (n + b - 1) / b;
+  std::vector<int> xv(n, -1);   // registers of solution values finished in this block
+  // forward: x_r -= sum over k < r of L(r, k) x_k, ascending k
+  for (int ib = 0; ib < nb; ++ib) {
+    const int i0 = ib * b, i1 = std::min(n, i0 + b);
+    std::vector<int> acc(b);
+    for (int i = i0; i < i1; ++i) acc[i - i0] = x.load(sl.xs + i);
+    for (int k = 0; k < i0; ++k) {
+      int xk = -1;
+      for (int i = i0; i < i1; ++i) {
+        const int q = P.at(i, k);
+        if (q < 0) continue;
+        if (xk < 0) xk = x.load(sl.xs + k);
+        acc[i - i0] = x.fma(x.neg(x.load(sl.lu + q)), xk, acc[i - i0]);
+      }
+    }
+    for (int i = i0; i < i1; ++i) {
+      for (int k = i0; k < i; ++k) {
+        const int q = P.at(i, k);
+        if (q >= 0) acc[i - i0] = x.fma(x.neg(x.load(sl.lu + q)), acc[k - i0], acc[i - i0]);
+      }
+      x.store(sl.xs + i, acc[i - i0]);
+    }
+  }
+  // backward: x_r = (x_r - sum over j > r of U(r, j) x_j) / pivot, ascending j
+  for (int ib = nb - 1; ib >= 0; --ib) {
+    const int i0 = ib * b, i1 = std::min(n, i0 + b);
+    std::vector<int> ext(n, -1);
+    for (int r = i1 - 1; r >= i0; --r) {
+      int acc = x.load(sl.xs + r);
+      for (int q = t.lu_diag[r] + 1; q < t.lu_row_ptr[r + 1]; ++q) {
+        const int j = t.lu_col[q];
+        int xj;
+        if (j < i1) {
+          xj = xv[j];
+        } else {
+          if (ext[j] < 0) ext[j] = x.load(sl.xs + j);
+          xj = ext[j];
+        }
+        acc = x.fma(x.neg(x.load(sl.lu + q)), xj, acc);
+      }
+      xv[r] = x.mul(acc, x.load(sl.lu + t.lu_diag[r]));
+      x.store(sl.xs + r, xv[r]);
+    }
+  }
+}
+
+std::string function(const char* name, const char* params, const Ptx& x, const char* prologue) {
+  std::string s;
+  s.reserve(x.body.size() + 512);
+  s += ".visible .func ";
+  s += name;
+  s += "(";
+  s += params;
+  s += ")\n{\n\t.reg .f64 %d<" + std::to_string(x.next + 1) + ">;\n\t.reg .b64 %p;\n\t.reg .b64 %b;\n"
+       "\t.reg .b64 %a;\n";
+  s += prologue;
+  s += x.body;
+  s += "\tret;\n}\n";
+  return s;
+}
+
+}  // namespace
+
+std::string generate_ptx(const HostTables& t, const GenOptions& o, int64_t* fma_count) {
+  if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64)
+    throw std::invalid_argument("tile sizes out of range");
+  const ScratchLayout sl = layout_of(t);
+  const Pattern P = pattern_of(t);
+  Ptx f;
+  int64_t nfma = 0;
+  emit_factor(f, t, sl, P, o.tile, &nfma);
+  if (nfma != t.lu_fma) throw std::logic_error("generated factorization does not match the symbolic count");
+  if (fma_count) *fma_count = nfma;
+  Ptx s;
+  emit_solve(s, t, sl, P, o.solve_block);
+  std::string out = ".version 9.0\n.target sm_103a\n.address_size 64\n\n";
+  out += function("fo_gen_factor", ".param .b64 fo_gen_factor_base, .param .b64 fo_gen_factor_alpha", f,
+                  "\tld.param.b64 %p, [fo_gen_factor_base];\n\tld.param.b64 %a, [fo_gen_factor_alpha];\n"
+                  "\tmov.b64 %d0, %a;\n\tcvta.to.global.u64 %b, %p;\n");
+  out += "\n";
+  out += function("fo_gen_solve", ".param .b64 fo_gen_solve_base", s,
+                  "\tld.param.b64 %p, [fo_gen_solve_base];\n\tcvta.to.global.u64 %b, %p;\n");
+  return out;
+}
+
+}  // namespace fo

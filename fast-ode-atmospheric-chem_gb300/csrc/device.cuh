@@ -1,6 +1,8 @@
 // Device-side data structures shared by the kernels of the integrator.
 #pragma once
 
+#include <vector_types.h>
+
 #include <cstdint>
 
 #include "stream.h"
@@ -77,6 +79,7 @@ struct DevOptions {
 // Per-lane scratch layout, in items (each item is `lanes` doubles).
 struct ScratchLayout {
   int64_t lu, negj, d, r, y, ynew, f0, ft, yr, k;  // offsets
+  int64_t xs;                                      // the generated solves' vector (n items)
   int64_t items;                                   // total items per lane
 };
 

@@ -23,6 +23,8 @@
 // values use FMA.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "rosenbrock.cuh"
 
 namespace fo {
@@ -84,13 +86,37 @@ __global__ void eval_kernel(SolveParams p, int C, int want_jac, double* out) {
 
 // ---- launch wrappers ----------------------------------------------------------
 
-cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream) {
-  static int configured_smem = -1;
-  if ((int)smem > 48 * 1024 && (int)smem != configured_smem) {
-    cudaError_t e = cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// The dynamic shared-memory limit above 48 KB is an attribute of a kernel on
+// one device: it is set once per (kernel, device) for the largest size asked
+// so far, under a lock, so a process that drives several devices, or several
+// host threads, never launches on a device where it was not set.
+class SmemAttribute {
+ public:
+  explicit SmemAttribute(const void* kernel) : kernel_(kernel) {}
+  cudaError_t ensure(size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    configured_smem = (int)smem;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mutex_);
+    if ((int)smem <= configured_[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) configured_[dev] = (int)smem;
+    return e;
   }
+
+ private:
+  static constexpr int kMaxDevices = 64;
+  const void* kernel_;
+  std::mutex mutex_;
+  int configured_[kMaxDevices] = {};
+};
+
+cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream) {
+  static SmemAttribute attribute(reinterpret_cast<const void*>(solve_kernel));
+  cudaError_t e = attribute.ensure(smem);
+  if (e != cudaSuccess) return e;
   solve_kernel<<<grid, p.lanes, smem, stream>>>(p);
   return cudaGetLastError();
 }
@@ -122,14 +148,10 @@ __global__ void __maxnreg__(255) solve_multi_kernel(const SolveParams* __restric
 cudaError_t launch_solve_multi(const SolveParams* batches, int nb, const int32_t* starts, int32_t* queue,
                                double* scratch, int64_t slot_doubles, int grid, int lanes, size_t smem,
                                cudaStream_t stream) {
-  static int configured_smem = -1;
-  if ((int)smem > 48 * 1024 && (int)smem != configured_smem) {
-    cudaError_t e =
-        cudaFuncSetAttribute(solve_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured_smem = (int)smem;
-  }
-  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int32_t), stream);
+  static SmemAttribute attribute(reinterpret_cast<const void*>(solve_multi_kernel));
+  cudaError_t e = attribute.ensure(smem);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(queue, 0, sizeof(int32_t), stream);
   if (e != cudaSuccess) return e;
   solve_multi_kernel<<<grid, lanes, smem, stream>>>(batches, nb, starts, queue, scratch, slot_doubles);
   return cudaGetLastError();

@@ -15,6 +15,13 @@
 #include "device.cuh"
 #include "fastode_gb300.h"
 
+#ifdef FO_LINK_GENERATED
+// The mechanism's generated factorization and solves (codegen.cpp), linked in
+// per mechanism: `base` is this lane's item 0 of its scratch slot (32 lanes).
+extern "C" __device__ void fo_gen_factor(double* base, double alpha);
+extern "C" __device__ void fo_gen_solve(double* base);
+#endif
+
 namespace fo {
 // internal linkage: every translation unit that includes this file keeps its
 // own copy of these device functions
@@ -573,8 +580,32 @@ __device__ void lu_solve(const SolveParams& p, const Lane& ln, const double* lu,
   }
 }
 
+// The generated variant (FO_VARIANT_GENERATED) exists only in the kernels
+// linked per mechanism with the generated functions.
+// Those kernels run nothing else (the launch code guarantees the variant),
+// so the other variants' factorizations and solves are not compiled into
+// them.
+__device__ __forceinline__ bool generated(const SolveParams&) {
+#ifdef FO_LINK_GENERATED
+  return true;
+#else
+  return false;
+#endif
+}
+
+// The variants that solve a per-lane vector in place rather than the work row.
+__device__ __forceinline__ bool solves_in_place(const SolveParams& p) {
+  return p.o.variant == FO_VARIANT_COMPACT || generated(p);
+}
+
 __device__ void factor_any(const SolveParams& p, const Lane& ln, double alpha, const double* negj, double* lu,
                            double* w, bool alg_only) {
+#ifdef FO_LINK_GENERATED
+  // the projection's algebraic-rows-only matrix takes the row loop (the same
+  // factors, in the same storage, bit for bit)
+  if (alg_only) factor(p, ln, alpha, negj, lu, w, alg_only);
+  else fo_gen_factor(lu - p.sl.lu * ln.L + ln.lane, alpha);
+#else
   if (p.o.variant == FO_VARIANT_PLAIN) factor(p, ln, alpha, negj, lu, w, alg_only);
   else if (p.o.variant == FO_VARIANT_COMPACT) {
     if (ln.L == 32) factor_compact<32>(p, ln, alpha, negj, lu, w, alg_only);
@@ -583,6 +614,7 @@ __device__ void factor_any(const SolveParams& p, const Lane& ln, double alpha, c
     if (ln.L == 32) factor_stream<32>(p, ln, alpha, negj, lu, w, alg_only);
     else factor_stream<0>(p, ln, alpha, negj, lu, w, alg_only);
   }
+#endif
 }
 
 __device__ __forceinline__ void solve_in_w(const SolveParams& p, const Lane& ln, const double* lu, double* w) {
@@ -594,6 +626,16 @@ __device__ __forceinline__ void solve_in_w(const SolveParams& p, const Lane& ln,
 // x = A^-1 b with the factors in lu (b and x per-lane vectors, may alias).
 __device__ void solve_into(const SolveParams& p, const Lane& ln, const double* lu, double* w, const double* b,
                            double* x) {
+#ifdef FO_LINK_GENERATED
+  // the generated solves work on the slot's solve vector (item xs), whose
+  // offset they know, so every access is an immediate offset from one base
+  const int L = ln.L, lane = ln.lane;
+  double* base = const_cast<double*>(lu) - p.sl.lu * L;
+  double* xs = base + p.sl.xs * L;
+  for (int i = 0; i < p.t.n; ++i) SCR(xs, i) = SCR(b, i);
+  fo_gen_solve(base + lane);
+  for (int i = 0; i < p.t.n; ++i) SCR(x, i) = SCR(xs, i);
+#else
   if (p.o.variant == FO_VARIANT_COMPACT) {
     lu_solve_compact(p, ln, lu, w, b, x);
     return;
@@ -602,6 +644,7 @@ __device__ void solve_into(const SolveParams& p, const Lane& ln, const double* l
   for (int i = 0; i < p.t.n; ++i) WROW(i) = SCR(b, i);
   solve_in_w(p, ln, lu, w);
   for (int i = 0; i < p.t.n; ++i) SCR(x, i) = WROW(i);
+#endif
 }
 
 // Sum over the block of one value per thread; every thread gets the same
@@ -648,7 +691,7 @@ __device__ __noinline__ double attempt(const SolveParams& p, const Lane& ln, dou
       forcing = Ft;
     }
     double* Kr = K + (int64_t)r * n * L;
-    const bool compact = p.o.variant == FO_VARIANT_COMPACT;   // right-hand side in Kr, solved in place
+    const bool in_place = solves_in_place(p);   // right-hand side in Kr, solved in place
     for (int i = 0; i < n; ++i) {
       double v = SCR(forcing, i);
       for (int s = 0; s < r; ++s) {
@@ -659,11 +702,11 @@ __device__ __noinline__ double attempt(const SolveParams& p, const Lane& ln, dou
           v = __dadd_rn(v, __dmul_rn(coef, ks));
         }
       }
-      if (compact) SCR(Kr, i) = v;
+      if (in_place) SCR(Kr, i) = v;
       else WROW(i) = v;
     }
-    if (compact) {
-      lu_solve_compact(p, ln, lu, w, Kr, Kr);
+    if (in_place) {
+      solve_into(p, ln, lu, w, Kr, Kr);
     } else {
       solve_in_w(p, ln, lu, w);
       for (int i = 0; i < n; ++i) SCR(Kr, i) = WROW(i);
@@ -1007,7 +1050,7 @@ __device__ __noinline__ void solve_group_backward_euler(const SolveParams& p, in
   double* dd = scr + p.sl.d * L;
   double* rr = scr + p.sl.r * L;
   double* lu = scr + p.sl.lu * L;
-  const bool compact = p.o.variant == FO_VARIANT_COMPACT;   // Newton update solved in place in F
+  const bool in_place = solves_in_place(p);   // Newton update solved in place in F
   for (int i = 0; i < n; ++i) {
     const double v = p.Y[ln.cell * p.ycs + (int64_t)__ldg(p.t.perm + i) * p.yss];
     SCR(Yn, i) = v;
@@ -1033,16 +1076,16 @@ __device__ __noinline__ void solve_group_backward_euler(const SolveParams& p, in
       ++c_lu;
       for (int i = 0; i < n; ++i) {
         const double v = __dsub_rn(SCR(F, i), __ddiv_rn(__dsub_rn(SCR(Yn1, i), SCR(Yn, i)), H));
-        if (compact) SCR(F, i) = v;
+        if (in_place) SCR(F, i) = v;
         else WROW(i) = v;
       }
-      if (compact) lu_solve_compact(p, ln, lu, w, F, F);
+      if (in_place) solve_into(p, ln, lu, w, F, F);
       else solve_in_w(p, ln, lu, w);
       ++c_solves;
       ++iterations;
       bool conv = true;
       for (int i = 0; i < n; ++i) {
-        const double d = compact ? SCR(F, i) : WROW(i);
+        const double d = in_place ? SCR(F, i) : WROW(i);
         const double y = clamp0(__dadd_rn(SCR(Yn1, i), d));
         SCR(Yn1, i) = y;
         if (iterations > 1) {

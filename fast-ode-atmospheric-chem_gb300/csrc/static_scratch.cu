@@ -12,7 +12,10 @@
 // The array's name is only a host-side stand-in in host code: its device
 // address is obtained once per device with cudaGetSymbolAddress, on the first
 // call made while that device is current, and passed to the kernel. That
-// first call should therefore be made before any stream capture begins.
+// first call should therefore be made before any stream capture begins. The
+// address is kept for the life of the process: after cudaDeviceReset, which
+// destroys the primary context and with it the module, the array may move, so
+// the entry point must not be used again in that process.
 //
 // All calls share the one array and it keeps the last call's contents; the
 // only state that must start at zero, the queue counter of the persistent

@@ -6,6 +6,9 @@
 // fo_update_photolysis: photolysis columns J * f(t) at an interval start, the
 // device form of the photolysis patch in fastode/ts1.py:204-214 (the factor is
 // the diurnal cosine max(0, cos(phase + omega t)) per cell).
+// fo_photolysis_factor: the same columns from per-cell factors f[c] computed by
+// the caller, k = J * f as one IEEE product, so a caller whose factors came
+// from the host gets the host's rate constants bit for bit.
 // fo_fp64_fma_rate: a DFMA throughput kernel that states the FP64 roofline
 // denominator on the device the integrator runs on.
 #include <cuda_runtime.h>
@@ -53,6 +56,16 @@ __global__ void photolysis_clock_kernel(int C, int nphoto, const int32_t* __rest
   k[(int64_t)c * kcs + (int64_t)rxn[p] * krs] = J[p] * (f > 0.0 ? f : 0.0);
 }
 
+__global__ void photolysis_factor_kernel(int C, int nphoto, const int32_t* __restrict__ rxn,
+                                         const double* __restrict__ J, const double* __restrict__ f,
+                                         double* __restrict__ k, int64_t kcs, int64_t krs) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)C * nphoto) return;
+  const int c = (int)(idx % C);
+  const int p = (int)(idx / C);
+  k[(int64_t)c * kcs + (int64_t)rxn[p] * krs] = __dmul_rn(J[p], f[c]);
+}
+
 __global__ void advance_clock_kernel(double* t_dev, double dt) { t_dev[0] += dt; }
 
 // Eight independent FMA chains per thread; every warp is full.
@@ -92,6 +105,17 @@ int fo_update_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const do
   const int block = 256;
   photolysis_kernel<<<(unsigned)((total + block - 1) / block), block, 0, (cudaStream_t)stream>>>(
       C, nphoto, rxn, J, phase, omega * t, k, k_cell_stride, k_reaction_stride);
+  return cudaGetLastError() == cudaSuccess ? FO_OK : FO_E_CUDA;
+}
+
+int fo_photolysis_factor(int32_t C, int32_t nphoto, const int32_t* rxn, const double* J, const double* f,
+                         double* k, int64_t k_cell_stride, int64_t k_reaction_stride, void* stream) {
+  if (C < 0 || nphoto < 0 || (nphoto > 0 && C > 0 && (!rxn || !J || !f || !k))) return FO_E_INVALID;
+  const int64_t total = (int64_t)C * nphoto;
+  if (total == 0) return FO_OK;
+  const int block = 256;
+  photolysis_factor_kernel<<<(unsigned)((total + block - 1) / block), block, 0, (cudaStream_t)stream>>>(
+      C, nphoto, rxn, J, f, k, k_cell_stride, k_reaction_stride);
   return cudaGetLastError() == cudaSuccess ? FO_OK : FO_E_CUDA;
 }
 

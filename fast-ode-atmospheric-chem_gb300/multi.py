@@ -60,14 +60,19 @@ class Part:
                           torch.as_tensor(np.asarray(phase, dtype=np.float64)).to(dev))
 
     def desc(self) -> _abi.BatchDesc:
-        return _abi.BatchDesc(self.plan.handle.value, self.alg.options(), self.ngroups, self.offsets.data_ptr(),
+        o = self.alg.options()
+        if o.variant == _abi.VARIANTS["generated"]:
+            # one launch runs several mechanisms: the table-driven kernel
+            o.variant = _abi.VARIANTS["compact"]
+        return _abi.BatchDesc(self.plan.handle.value, o, self.ngroups, self.offsets.data_ptr(),
                               self.max_cells, self.Y.data_ptr(), 1, self.C, self.k.data_ptr(), 1, self.C,
                               self.atol.data_ptr(), self.rtol, self.dt, self.memory.data_ptr(),
                               self.counts.data_ptr(), self.status.data_ptr())
 
     def smem_per_block(self) -> int:
         lanes = ((self.max_cells + 31) // 32) * 32
-        return 8 * (32 + self.plan.smem_items(getattr(self.alg, "kernel", "pipelined")) * lanes)
+        kernel = getattr(self.alg, "kernel", "pipelined")
+        return 8 * (32 + self.plan.smem_items("compact" if kernel == "generated" else kernel) * lanes)
 
     def reset(self):
         self.Y.copy_(self.Y0)

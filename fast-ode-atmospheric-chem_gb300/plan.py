@@ -80,6 +80,30 @@ class Plan:
         _abi.check(_abi.lib().fo_plan_permutation(handle, _ptr(perm, C.c_int32)), "fo_plan_permutation")
         self.perm = perm
         self._workspaces = {}
+        self.gen_info = None
+
+    def generate(self, cache_dir=None) -> dict:
+        """Prepare the generated variant (fo_plan_generate): the mechanism's
+        factorization and solves as straight-line code linked with the
+        integrator, cached on disk; idempotent. Returns what it did."""
+        if self.gen_info is None:
+            info = _abi.GenInfo()
+            arg = None if cache_dir is None else str(cache_dir).encode()
+            _abi.check(_abi.lib().fo_plan_generate(self.handle, arg, C.byref(info)), "fo_plan_generate")
+            self.gen_info = info.as_dict()
+        return self.gen_info
+
+    def options_for(self, algorithm, max_group_cells: int):
+        """The fo_options of `algorithm` for groups of up to `max_group_cells`
+        cells. The generated variant prepares this plan first; it runs groups
+        of at most 32 cells, so larger groups take the compact variant."""
+        o = algorithm.options()
+        if algorithm.kernel == "generated":
+            if max_group_cells <= 32:
+                self.generate()
+            else:
+                o.variant = _abi.VARIANTS["compact"]
+        return o
 
     @property
     def has_constraints(self) -> bool:

@@ -103,7 +103,7 @@ def _device_solve(solver, system, Y, dt, atol, rtol, counts: Counts, mem):
     ws = plan.workspace(1, C_cells)
     stream = torch.cuda.current_stream(dev)
     rc = _abi.lib().fo_solve(
-        plan.handle, C.byref(solver.options()), 1, offs.data_ptr(), C_cells,
+        plan.handle, C.byref(plan.options_for(solver, C_cells)), 1, offs.data_ptr(), C_cells,
         Yd.data_ptr(), n, 1, kd.data_ptr(), 0 if k.shape[0] == 1 else plan.R, 1,
         atold.data_ptr(), float(rtol), float(dt),
         memd.data_ptr(), cnt.data_ptr(), st.data_ptr(), ws.data_ptr(), ws.numel(), 0,
@@ -127,12 +127,15 @@ class Algorithm:
                  carry: bool = True, quantize: bool = True, max_steps: int = 1000,
                  carry_memory: bool = True, ordering: str = "auto", kernel: str = "compact"):
         """The reference's arguments, plus two of the device path: the
-        fill-reducing ``ordering`` of the sparse LU and the ``kernel`` variant
-        ("compact", the fast path, which keeps half a row and half the solve
-        vector in shared memory so twice as many groups stay resident;
-        "pipelined", whole rows in shared memory; or "plain", the direct
-        loops). The three give the same factors; the solves differ in
-        summation order."""
+        fill-reducing ``ordering`` of the sparse LU and the ``kernel`` variant:
+        "generated", the mechanism's own factorization and solves generated as
+        straight-line code when its plan is first used (compiled once, then
+        cached on disk; groups of at most 32 cells, larger groups run
+        "compact"); "compact", table-driven, half a row and half the solve
+        vector in shared memory; "pipelined", whole rows in shared memory; or
+        "plain", the direct loops. All give the same factors; "generated" and
+        "plain" give the same solutions bit for bit, the others differ in the
+        solves' summation order."""
         self.tableau = tableau
         self.controller = controller
         self.b = b

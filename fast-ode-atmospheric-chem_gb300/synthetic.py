@@ -222,6 +222,20 @@ def dae_constrained(n_cells: int = 16384, intervals: int = 120, seed: int = 5, n
                        mass=mass)
 
 
+def photolysis_factors(cells: SyntheticCells, dt: float, intervals: int) -> np.ndarray:
+    """(intervals, C) diurnal factors f of every interval start t = i * dt, as
+    ``rate_constants`` computes them; photolysis column j of interval i is
+    then J[j] * f[i] (one IEEE product, reproduced exactly on the device)."""
+    return np.stack([diurnal_factor(cells, i * dt) for i in range(intervals)])
+
+
+# The seeded parity subset of the 210/500, 65,536-cell workload: eight whole
+# groups of 32 cells spread over the 2,048 groups. The reference is run on
+# these groups (tests/golden/ros3_210x500_subset.npz) and the measured run is
+# checked against it on the same groups.
+PLAIN_LARGE_PARITY_GROUPS = (0, 292, 585, 877, 1170, 1462, 1755, 2047)
+
+
 def plain_large(n_cells: int = 65536, intervals: int = 120, seed: int = 2) -> Workload:
     """Plain ROS3, 210 species / 500 reactions, 65,536 cells in groups of 32,
     T U[200, 310] K, p U[10, 1000] hPa setting [M], dt = 30 s x 120 intervals,

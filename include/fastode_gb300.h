@@ -169,6 +169,23 @@ typedef struct fo_options {
  * The factors are those of PIPELINED bit for bit; the solves differ in
  * summation order (roundoff). fo_adjoint_interval runs PIPELINED. */
 #define FO_VARIANT_COMPACT 2
+/* GENERATED runs the mechanism's own factorization and solves, generated as
+ * straight-line code from its fill pattern and compiled when the plan is
+ * prepared with fo_plan_generate (register tiles of the factorization, every
+ * operand at an immediate offset, no schedule tables). Groups of at most 32
+ * cells. Factors and solutions are those of PLAIN bit for bit. */
+#define FO_VARIANT_GENERATED 3
+
+/* What fo_plan_generate did. */
+typedef struct {
+  int32_t from_cache;    /* 1: the linked module was read from the cache */
+  int32_t registers;     /* registers per thread of the generated kernel */
+  int32_t tile;          /* rows and columns of the factorization's register tiles */
+  int32_t local_bytes;   /* local memory per thread (spills) of the generated kernel */
+  double seconds;        /* host time: generation, linking (or cache read) and loading */
+  int64_t ptx_bytes;     /* size of the generated PTX */
+  int64_t cubin_bytes;   /* size of the linked module */
+} fo_gen_info;
 
 /* Host-only symbolic analysis: ordering, fill and flop counts, and (when
  * perm is not NULL) the elimination order perm[p] = species eliminated p-th.
@@ -186,6 +203,26 @@ int fo_plan_destroy(fo_plan* plan);
 
 /* The permutation chosen by the ordering: perm[p] = species eliminated p-th (host, n). */
 int fo_plan_permutation(const fo_plan* plan, int32_t* perm);
+
+/* Prepare a plan for FO_VARIANT_GENERATED: generate the mechanism's
+ * factorization of alpha*M - J and its triangular solves as straight-line PTX
+ * from the plan's fill pattern (the per-mechanism form of
+ * fastode/linalg.py:70-81 and of the Jacobian assembly of
+ * fastode/linalg.py:60-67), link it with the library's integrator kernel
+ * (nvJitLink, opened at run time) and load the module on the current device.
+ * The linked module is cached in cache_dir under a hash of its inputs (NULL:
+ * $FASTODE_GB300_CACHE, else $XDG_CACHE_HOME/fastode_gb300, else
+ * ~/.cache/fastode_gb300; "": no cache). Linking compiles the generated code:
+ * about a minute for 200,000 multiply-adds; a cached module loads in
+ * milliseconds. info may be NULL. Idempotent. Returns FO_E_UNSUPPORTED when
+ * nvJitLink is missing or linking fails (fo_last_error has the log). */
+int fo_plan_generate(fo_plan* plan, const char* cache_dir, fo_gen_info* info);
+
+/* Host-only check of the generated variant (no device needed): generate the
+ * mechanism's code for the given ordering and, when link is nonzero, link it
+ * with the integrator (nvJitLink); info gets the sizes and the time taken.
+ * No counterpart in the reference. */
+int fo_generate_check(const fo_mechanism_desc* mech, int32_t ordering, int32_t link, fo_gen_info* info);
 
 /* Bytes of device workspace fo_solve needs for `slots` groups in flight
  * of at most `max_group_cells` cells each (see fo_solve). */
@@ -335,6 +372,15 @@ int fo_update_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const do
                          const double* phase, double omega, double t, double* k,
                          int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
 
+/* Photolysis columns at an interval start from per-cell factors the caller
+ * computed: k[c, rxn[p]] = J[p] * f[c], one correctly rounded product, which
+ * is the assignment k[:, photo] = J[None, photo] * f[:, None] of a host rate
+ * constant builder (the per-interval photolysis patch of
+ * fastode/ts1.py:204-214 with the diurnal factor evaluated by the caller).
+ * Device pointers; asynchronous on stream. */
+int fo_photolysis_factor(int32_t C, int32_t nphoto, const int32_t* rxn, const double* J, const double* f,
+                         double* k, int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
+
 /* Photolysis columns of one interval of a TS1 scenario:
  * k(c, rxn[p]) = (base[p * C + c] * factor) * scaling[p], the per-interval
  * patch of fastode/ts1.py:204-214 (run_scenario sets params[name] = base * f
@@ -388,13 +434,18 @@ int fo_fp64_fma_rate(double* fma_per_second);
  * cudaMalloc/cudaFree. The caller still passes every input and output (same
  * meaning as fo_solve); the scratch is one file-scope device array of
  * FO_STATIC_SCRATCH_BYTES (32 MiB) that every GPU loading the library holds
- * until the process exits, holding as many groups in flight as fit (a
- * 210-species / 500-reaction group of 32 cells needs about 4.9 MB, so six at a
- * time). A mechanism whose single group does not fit is rejected with
- * FO_E_UNSUPPORTED. The first call on each device looks up the array's device
- * address and should come before any stream capture. All calls share the array:
- * calls whose kernels overlap on the GPU race on it, so order them on one
- * stream.
+ * until the process exits, holding as many groups in flight as fit: one slot
+ * per group in flight, of fo_workspace_bytes(plan, 2, C) -
+ * fo_workspace_bytes(plan, 1, C) bytes (a 210-species / 500-reaction group of
+ * 32 cells needs about 4.2 MB, so eight at a time); more groups than slots are
+ * pulled from a device queue by the slots in turn. A mechanism whose single
+ * group does not fit is rejected with FO_E_UNSUPPORTED. The first call on each
+ * device looks up the array's device address and should come before any stream
+ * capture; the address is kept for the life of the process, so after
+ * cudaDeviceReset (or anything else that destroys the device's primary
+ * context) this entry point must not be called again in that process. All
+ * calls share the array: calls whose kernels overlap on the GPU race on it, so
+ * order them on one stream.
  */
 int fo_solve_static(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
                     int32_t max_group_cells, double* Y, int64_t y_cell_stride, int64_t y_species_stride,

@@ -18,6 +18,7 @@ status codes per group and interval, final Memory per group, and the
 from __future__ import annotations
 
 import argparse
+import os
 import sys
 from pathlib import Path
 
@@ -271,10 +272,109 @@ def backward_euler_ts1(reference):
     return out
 
 
+SUBSET_INTERVALS = 30
+SUBSET_SNAPSHOTS = (10, 20, 30)
+
+
+def _subset_group(args):
+    """One group of the 210/500 parity subset through the reference: cumulative
+    Counts and status after every interval, the (H, err) of every attempt with
+    the interval it belongs to, the state at the snapshot intervals and the
+    final Memory."""
+    reference, root, Y0, k0, photo, J, f, dt, atol, rtol, intervals = args
+    sys.path.insert(0, reference)
+    sys.path.insert(0, root)
+    from fastode import Algorithm, Counts, ROS3
+    from fastode.chem import ChemSystem, Mechanism
+    import fastode.solvers as S
+    from fastode_gb300 import synthetic as syn
+    wl = syn.plain_large(n_cells=32, intervals=1)
+    rm = Mechanism(wl.sm.species, wl.sm.reactions)
+    hs, errs, where = [], [], []
+    cur = [0]
+    original, original_stages = S.error_norm, S.stages
+
+    def traced(Yv, Ynew, E, at, rt):
+        e = original(Yv, Ynew, E, at, rt)
+        errs.append(e)
+        where.append(cur[0])
+        return e
+
+    def traced_stages(system, tab, Yv, F0, LU, H, cnt):
+        hs.append(H)
+        return original_stages(system, tab, Yv, F0, LU, H, cnt)
+
+    S.error_norm, S.stages = traced, traced_stages
+    alg = Algorithm(ROS3)
+    mem = alg.new_memory()
+    c = Counts()
+    Y = Y0.copy()
+    counts, status, snaps = [], [], {}
+    for i in range(intervals):
+        cur[0] = i
+        k = k0.copy()
+        k[:, photo] = J[None, :] * f[i][:, None]
+        Y, st = alg.solve(ChemSystem(rm, k), Y, dt, atol, rtol, c, mem)
+        counts.append(list(c.as_dict().values()))
+        status.append(STATUS[st])
+        if i + 1 in SUBSET_SNAPSHOTS:
+            snaps[i + 1] = Y.copy()
+    return (np.array(counts), np.array(status), np.array(hs), np.array(errs), np.array(where),
+            np.stack([snaps[s] for s in SUBSET_SNAPSHOTS]), np.array([mem.h_next, mem.err_prev, mem.h_prev]))
+
+
+def c2_subset(reference):
+    """The reference on the seeded parity subset of the 210/500, 65,536-cell
+    workload (synthetic.PLAIN_LARGE_PARITY_GROUPS, eight whole groups) over
+    the first 30 intervals, one group per process. Stores the inputs of those
+    cells (Y0, k at t = 0, the photolysis columns and every interval's diurnal
+    factors), so that the device can consume exactly the reference's inputs."""
+    import multiprocessing as mp
+    from fastode_gb300 import synthetic as syn
+    wl = syn.plain_large()
+    groups = syn.PLAIN_LARGE_PARITY_GROUPS
+    gs = wl.group_size
+    cells = np.concatenate([np.arange(g * gs, (g + 1) * gs) for g in groups])
+    sub = wl.subset(cells)
+    k0 = sub.k_at(0)
+    photo = np.nonzero(wl.sm.photolytic)[0].astype(np.int32)
+    J = wl.sm.J[photo]
+    f = syn.photolysis_factors(sub.cells, wl.dt, SUBSET_INTERVALS)
+    for i in range(SUBSET_INTERVALS):          # the stored inputs rebuild k_at exactly
+        k = k0.copy()
+        k[:, photo] = J[None, :] * f[i][:, None]
+        assert np.array_equal(k, sub.k_at(i))
+    jobs = [(reference, str(ROOT), sub.cells.Y0[j * gs:(j + 1) * gs], k0[j * gs:(j + 1) * gs], photo, J,
+             f[:, j * gs:(j + 1) * gs], wl.dt, wl.atol, wl.rtol, SUBSET_INTERVALS) for j in range(len(groups))]
+    env = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS")}
+    os.environ["OMP_NUM_THREADS"] = os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    try:
+        with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+            res = pool.map(_subset_group, jobs)
+    finally:
+        for k, v in env.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    L = max(len(r[2]) for r in res)
+    pad = lambda a, fill: np.concatenate([a, np.full(L - len(a), fill, dtype=np.asarray(a).dtype)])
+    rt, pt, yt = reaction_tables(wl.sm)
+    return dict(n=wl.sm.n, reactants=rt, products=pt, yields=yt, groups=np.array(groups), cells=cells,
+                group_size=gs, Y0=sub.cells.Y0, k0=k0, photo=photo, J=J, f=f, dt=wl.dt,
+                intervals=SUBSET_INTERVALS, rtol=wl.rtol, atol=wl.atol,
+                counts=np.stack([r[0] for r in res]), status=np.stack([r[1] for r in res]),
+                hs=np.stack([pad(r[2], np.nan) for r in res]), errs=np.stack([pad(r[3], np.nan) for r in res]),
+                interval_of=np.stack([pad(r[4], -1) for r in res]),
+                n_attempts=np.array([len(r[2]) for r in res]), snapshots=np.array(SUBSET_SNAPSHOTS),
+                Y_snap=np.stack([r[5] for r in res], axis=1).reshape(len(SUBSET_SNAPSHOTS), -1, wl.sm.n),
+                memory=np.stack([r[6] for r in res]))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["backward-euler"], default=None,
+    ap.add_argument("--only", choices=["backward-euler", "c2-subset"], default=None,
                     help="regenerate one fixture instead of all")
     a = ap.parse_args()
     sys.path.insert(0, a.reference)
@@ -285,6 +385,14 @@ def main():
     if a.only == "backward-euler":
         np.savez_compressed(HERE / "ts1_tier1_30s_backward_euler.npz", **backward_euler_ts1(a.reference))
         return
+    if a.only == "c2-subset":
+        out = c2_subset(a.reference)
+        np.savez_compressed(HERE / "ros3_210x500_subset.npz", **out)
+        print("ros3_210x500_subset counts", out["counts"][:, -1].sum(axis=0).tolist(), "attempts",
+              out["n_attempts"].tolist())
+        return
+    out = c2_subset(a.reference)
+    np.savez_compressed(HERE / "ros3_210x500_subset.npz", **out)
     np.savez_compressed(HERE / "ts1_tier1_30s_backward_euler.npz", **backward_euler_ts1(a.reference))
 
     ts1 = ts1_case(a.reference)

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("case", DAE_CASES)
-@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact"])
+@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact", "generated"])
 def test_rodas3_projection_matches_reference(cuda, case, kernel):
     from fastode_gb300 import RODAS3, Algorithm, ChemSystem, Counts
     f = load(case)
@@ -51,7 +51,7 @@ def test_rodas3_projection_matches_reference(cuda, case, kernel):
     assert rel_err(Y, f["Y"], floor=1e-300 + np.abs(f["atol"]).max() * 1e-4).max() <= 1e-9
 
 
-@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact"])
+@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact", "generated"])
 def test_constrained_synthetic_matches_reference(cuda, kernel):
     """The constrained synthetic workload (150 differential + 10 quasi-steady
     species, one group of 32 cells, four 60 s intervals, RODAS3 at rtol 1e-4):

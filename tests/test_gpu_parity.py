@@ -47,7 +47,7 @@ def run_batch(cuda, f, trace_cap=64, slots=0, group_size=None, kernel="pipelined
 
 
 @pytest.mark.parametrize("case", CASES)
-@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact"])
+@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact", "generated"])
 def test_device_matches_reference_fixture(cuda, case, kernel):
     f = load(case)
     b, statuses, traces = run_batch(cuda, f, kernel=kernel)

@@ -178,7 +178,8 @@ def test_struct_layouts_match_the_header(tmp_path):
     if cc is None:
         pytest.skip("no host C compiler")
     structs = {"fo_options": _abi.Options, "fo_batch_desc": _abi.BatchDesc,
-               "fo_mechanism_desc": _abi.MechanismDesc, "fo_plan_info": _abi.PlanInfo}
+               "fo_mechanism_desc": _abi.MechanismDesc, "fo_plan_info": _abi.PlanInfo,
+               "fo_gen_info": _abi.GenInfo}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fastode_gb300.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
@@ -287,3 +288,32 @@ def test_large_mechanism_falls_back_from_the_stream_kernels(built_library):
     assert time.perf_counter() - t0 < 30.0
     assert info["nnz_lu"] > 65536
     assert info["compact_smem_doubles_per_cell"] == info["smem_doubles_per_cell"]
+
+
+def _gen_check(mech, link):
+    from fastode_gb300 import _abi
+    from fastode_gb300.plan import _Desc
+    d = _Desc(mech)
+    info = _abi.GenInfo()
+    rc = _abi.lib().fo_generate_check(ctypes.byref(d.desc), _abi.ORDERINGS["auto"], int(link), ctypes.byref(info))
+    return rc, info.as_dict(), _abi.lib().fo_last_error().decode()
+
+
+def test_generated_code_links_with_the_integrator(built_library):
+    """The generated variant of a small mechanism: its PTX is generated (the
+    generator checks its multiply-add count against the symbolic analysis)
+    and links with the library's relocatable integrator (nvJitLink, no
+    device needed)."""
+    from fastode_gb300 import synthetic as syn
+    rc, info, err = _gen_check(syn.plain_small().sm.mech, link=True)
+    assert rc == 0, err
+    assert info["ptx_bytes"] > 0 and info["cubin_bytes"] > 0 and info["tile"] == 6
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_generated_code_covers_every_update(built_library, case):
+    """Generation alone (no link) for the fixtures' mechanisms, the 210/500
+    one included: one fused multiply-add per update of the symbolic LU."""
+    rc, info, err = _gen_check(mechanism_of(load(case)), link=False)
+    assert rc == 0, err
+    assert info["ptx_bytes"] > 0
