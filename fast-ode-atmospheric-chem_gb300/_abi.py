@@ -68,6 +68,13 @@ class GenInfo(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class RateLaw(C.Structure):
+    _fields_ = [("type", C.c_int32), ("column", C.c_int32), ("c", C.c_double * 8)]
+
+
+RATE_ARRHENIUS, RATE_TROE, RATE_USER, RATE_SURFACE = 0, 1, 2, 3
+
+
 class BatchDesc(C.Structure):
     _fields_ = [("plan", C.c_void_p), ("opt", Options), ("ngroups", C.c_int32),
                 ("group_offsets", C.c_void_p), ("max_group_cells", C.c_int32),
@@ -103,6 +110,7 @@ SIGNATURES = {
     "fo_rate_constants": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
     "fo_update_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _D, _P, _I64, _I64, _P]),
     "fo_photolysis_factor": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _I64, _I64, _P]),
+    "fo_rate_laws": (C.c_int, [_I32, _I32, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _P]),
     "fo_fp64_fma_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "fo_scale_photolysis": (C.c_int, [_I32, _I32, _P, _P, _P, _D, _P, _I64, _I64, _P]),
     "fo_score_accumulate": (C.c_int, [_I32, _I32, _P, _I64, _I64, _I32, _P, _P, _I64, _I64, _D, _I32,

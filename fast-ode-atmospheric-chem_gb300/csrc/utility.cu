@@ -9,9 +9,12 @@
 // fo_photolysis_factor: the same columns from per-cell factors f[c] computed by
 // the caller, k = J * f as one IEEE product, so a caller whose factors came
 // from the host gets the host's rate constants bit for bit.
+// fo_rate_laws: every rate constant of a TS1-style mechanism (Arrhenius,
+// Troe, user-defined and surface rows, the third-body fold) on the device.
 // fo_fp64_fma_rate: a DFMA throughput kernel that states the FP64 roofline
 // denominator on the device the integrator runs on.
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include <cstdint>
 #include <string>
@@ -66,6 +69,77 @@ __global__ void photolysis_factor_kernel(int C, int nphoto, const int32_t* __res
   k[(int64_t)c * kcs + (int64_t)rxn[p] * krs] = __dmul_rn(J[p], f[c]);
 }
 
+// The universal gas constant as the reference forms it (fastode/ts1.py:30-32)
+// and pi as Python's math.pi.
+constexpr double kBoltzmann = 1.380649e-23;
+constexpr double kAvogadro = 6.02214076e23;
+constexpr double kRGas = kBoltzmann * kAvogadro;
+constexpr double kPi = 3.141592653589793;
+
+// x ** e for an array x and a scalar e, as NumPy evaluates it: -1, 0, 0.5, 1
+// and 2 by the reciprocal, one, the square root, x and the square; other
+// exponents by pow.
+__device__ double scalar_power(double x, double e) {
+  if (e == 1.0) return x;
+  if (e == -1.0) return __ddiv_rn(1.0, x);
+  if (e == 0.0) return 1.0;
+  if (e == 0.5) return __dsqrt_rn(x);
+  if (e == 2.0) return __dmul_rn(x, x);
+  return pow(x, e);
+}
+
+// One rate constant per thread, cells fastest (fastode/ts1.py:66-103, each
+// expression in the reference's order, no contraction).
+__global__ void rate_laws_kernel(int C, int R, const fo_rate_law* __restrict__ laws, const double* __restrict__ T,
+                                 const double* __restrict__ P, const double* __restrict__ params, int64_t pcs,
+                                 const double* __restrict__ power, double* __restrict__ k, int64_t kcs,
+                                 int64_t krs) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)C * R) return;
+  const int c = (int)(idx % C);
+  const int j = (int)(idx / C);
+  const fo_rate_law& L = laws[j];
+  const double t = T[c], p = P[c];
+  double v;
+  switch (L.type) {
+    case FO_RATE_ARRHENIUS:
+      v = __dmul_rn(__dmul_rn(__dmul_rn(L.c[0], exp(__ddiv_rn(L.c[2], t))), scalar_power(__ddiv_rn(t, L.c[3]), L.c[1])),
+                    __dadd_rn(1.0, __dmul_rn(L.c[4], p)));
+      break;
+    case FO_RATE_TROE: {
+      const double M = __ddiv_rn(p, __dmul_rn(kRGas, t));
+      const double k0 = __dmul_rn(__dmul_rn(L.c[0], exp(__ddiv_rn(L.c[2], t))), scalar_power(__ddiv_rn(t, 300.0), L.c[1]));
+      const double kinf =
+          __dmul_rn(__dmul_rn(L.c[3], exp(__ddiv_rn(L.c[5], t))), scalar_power(__ddiv_rn(t, 300.0), L.c[4]));
+      const double k0M = __dmul_rn(k0, M);
+      const double ratio = __ddiv_rn(k0M, kinf);
+      const double l = log10(ratio);
+      v = __dmul_rn(__ddiv_rn(k0M, __dadd_rn(1.0, ratio)), pow(L.c[6], __ddiv_rn(L.c[7], __dadd_rn(L.c[7], __dmul_rn(l, l)))));
+      break;
+    }
+    case FO_RATE_USER:
+      v = __dmul_rn(params[(int64_t)L.column * pcs + c], L.c[0]);
+      break;
+    case FO_RATE_SURFACE: {
+      const double radius = params[(int64_t)L.column * pcs + c];
+      const double number = params[(int64_t)(L.column + 1) * pcs + c];
+      const double speed = __dsqrt_rn(__dmul_rn(L.c[0], t));
+      const double num = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(4.0, number), kPi), radius), radius);
+      v = __ddiv_rn(num, __dadd_rn(__ddiv_rn(radius, L.c[1]), __ddiv_rn(4.0, __dmul_rn(speed, L.c[2]))));
+      break;
+    }
+    default:
+      v = CUDART_NAN;
+  }
+  if (power != nullptr && power[j] != 0.0) {
+    const double M = __ddiv_rn(p, __dmul_rn(kRGas, t));
+    const double e = power[j];
+    // M ** power with an array exponent: pow, exact for the exponents 1 and 2
+    v = __dmul_rn(v, e == 1.0 ? M : (e == 2.0 ? __dmul_rn(M, M) : pow(M, e)));
+  }
+  k[(int64_t)c * kcs + (int64_t)j * krs] = v;
+}
+
 __global__ void advance_clock_kernel(double* t_dev, double dt) { t_dev[0] += dt; }
 
 // Eight independent FMA chains per thread; every warp is full.
@@ -116,6 +190,19 @@ int fo_photolysis_factor(int32_t C, int32_t nphoto, const int32_t* rxn, const do
   const int block = 256;
   photolysis_factor_kernel<<<(unsigned)((total + block - 1) / block), block, 0, (cudaStream_t)stream>>>(
       C, nphoto, rxn, J, f, k, k_cell_stride, k_reaction_stride);
+  return cudaGetLastError() == cudaSuccess ? FO_OK : FO_E_CUDA;
+}
+
+int fo_rate_laws(int32_t C, int32_t R, const fo_rate_law* laws, const double* T, const double* P,
+                 const double* params, int64_t param_column_stride, const double* power, double* k,
+                 int64_t k_cell_stride, int64_t k_reaction_stride, void* stream) {
+  if (C < 0 || R < 0) return FO_E_INVALID;
+  const int64_t total = (int64_t)C * R;
+  if (total == 0) return FO_OK;
+  if (!laws || !T || !P || !k) return FO_E_INVALID;
+  const int block = 256;
+  rate_laws_kernel<<<(unsigned)((total + block - 1) / block), block, 0, (cudaStream_t)stream>>>(
+      C, R, laws, T, P, params, param_column_stride, power, k, k_cell_stride, k_reaction_stride);
   return cudaGetLastError() == cudaSuccess ? FO_OK : FO_E_CUDA;
 }
 

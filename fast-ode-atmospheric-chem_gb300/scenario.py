@@ -6,10 +6,13 @@ and ``TS1`` objects (or anything with the same attributes) and returns
 (snapshots, counts, statuses). Where the reference integrates one group after
 the other, here every group of the scenario advances in one ``fo_solve``
 launch per interval; groups never exchange data, so the results per group are
-the same. The rate constants are computed once on the host with
-``ts1.rate_constants`` (as the reference does at a group's first interval),
-the per-interval photolysis columns are patched on the device
-(``fo_scale_photolysis``), and snapshots are copies of the device state.
+the same. The rate constants of the first interval are evaluated on the
+device from the mechanism's rate laws (``rate_law_table``, ``fo_rate_laws``:
+Arrhenius, Troe, user-defined and surface rows and the third-body fold of
+fastode/ts1.py:66-103; a mechanism object without reaction records uses its
+own ``rate_constants``), the per-interval photolysis columns are patched on
+the device (``fo_scale_photolysis``), and snapshots are copies of the device
+state.
 
 ``score`` and ``digits`` are fastode.ts1.score (fastode/ts1.py:226-264) and
 fastode.reference.digits (fastode/reference.py:41-59): the reference table is
@@ -75,6 +78,81 @@ class _Photolysis:
             _abi.check(rc, "fo_scale_photolysis")
 
 
+RATE_DTYPE = np.dtype([("type", np.int32), ("column", np.int32), ("c", np.float64, (8,))])
+BOLTZMANN = 1.380649e-23
+AVOGADRO = 6.02214076e23
+R_GAS = BOLTZMANN * AVOGADRO
+
+
+def rate_law_table(ts1):
+    """The rate laws of a TS1-style mechanism as fo_rate_law records, compiled
+    from its reaction records (the keys and defaults fastode/ts1.py:72-98
+    reads), and the names of the per-cell parameters they read, in column
+    order. None when a reaction has a type the device does not evaluate."""
+    laws = np.zeros(len(ts1.reactions), dtype=RATE_DTYPE)
+    columns = []
+
+    def column(name):
+        if name not in columns:
+            columns.append(name)
+        return columns.index(name)
+
+    for j, r in enumerate(ts1.reactions):
+        t = r.get("type")
+        c = np.zeros(8)
+        col = -1
+        if t == "ARRHENIUS":
+            code = _abi.RATE_ARRHENIUS
+            c[:5] = [r.get("A", 1.0), r.get("B", 0.0), r.get("C", 0.0), r.get("D", 300.0), r.get("E", 0.0)]
+        elif t == "TROE":
+            code = _abi.RATE_TROE
+            c[:] = [r.get("k0_A", 1.0), r.get("k0_B", 0.0), r.get("k0_C", 0.0), r.get("kinf_A", 1.0),
+                    r.get("kinf_B", 0.0), r.get("kinf_C", 0.0), r.get("Fc", 0.6), r.get("N", 1.0)]
+        elif t == "USER_DEFINED":
+            code = _abi.RATE_USER
+            col = column(r["MUSICA name"])
+            c[0] = r.get("scaling factor", 1.0)
+        elif t == "SURFACE":
+            code = _abi.RATE_SURFACE
+            label = r["MUSICA name"]
+            col = column(label + ".effective radius [m]")
+            nxt = label + ".particle number concentration [# m-3]"
+            if nxt in columns or col != len(columns) - 1:
+                return None
+            columns.append(nxt)
+            sp = ts1.props[r["gas-phase reactant"]]
+            c[0] = 8.0 * R_GAS / (math.pi * sp["molecular weight [kg mol-1]"])
+            c[1] = sp["diffusion coefficient [m2 s-1]"]
+            c[2] = r.get("reaction probability", 1.0)
+        else:
+            return None
+        laws[j] = (code, col, c)
+    return laws, columns
+
+
+def device_rate_constants(ts1, T, P, params, dev, stream, table=None):
+    """(R, C) rate constants, cells fastest, evaluated on the device by
+    fo_rate_laws: fastode.ts1.TS1.rate_constants(T, P, params)
+    (fastode/ts1.py:66-103) without the host loop."""
+    torch = _torch()
+    laws, columns = table if table is not None else rate_law_table(ts1)
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    C_cells, R = len(T), len(laws)
+    d_laws = torch.from_numpy(np.frombuffer(laws.tobytes(), dtype=np.uint8).copy()).to(dev)
+    d_T = torch.from_numpy(T).to(dev)
+    d_P = torch.from_numpy(np.ascontiguousarray(P, dtype=np.float64)).to(dev)
+    mat = np.stack([np.asarray(params[nm], dtype=np.float64) for nm in columns]) if columns else np.zeros((1, C_cells))
+    d_par = torch.from_numpy(np.ascontiguousarray(mat)).to(dev)
+    power = np.asarray(ts1.mech.third_body_power, dtype=np.float64)
+    d_pow = torch.from_numpy(power).to(dev) if np.any(power) else None
+    k = torch.empty((R, C_cells), dtype=torch.float64, device=dev)
+    _abi.check(_abi.lib().fo_rate_laws(C_cells, R, d_laws.data_ptr(), d_T.data_ptr(), d_P.data_ptr(),
+                                       d_par.data_ptr(), C_cells, d_pow.data_ptr() if d_pow is not None else None,
+                                       k.data_ptr(), 1, C_cells, C.c_void_p(stream.cuda_stream)), "fo_rate_laws")
+    stream.synchronize()     # the uploads above are freed on return
+    return k
+
+
 def run_scenario(scenario, solver, cells, ts1, rtol, atol, group_size=32, constrained=(), warmup_steps=0,
                  steps=None, on_step=None, snapshots_on_device=False):
     """Run a solver on a scenario's cells in groups that share a step
@@ -97,12 +175,18 @@ def run_scenario(scenario, solver, cells, ts1, rtol, atol, group_size=32, constr
     params = dict(cells.params)
     for name in photolysis:
         params[name] = np.asarray(cells.params[name]) * f_first
-    k_static = np.asarray(ts1.rate_constants(cells.T, cells.P, params), dtype=np.float64)
     batch = Batch(ts1.mech, cells.Y, group_size=group_size, algorithm=solver,
                   mass=None if np.all(mass == 1.0) else mass)
     dev, Cc = batch.dev, batch.C
     stream = batch._stream()
-    k = torch.from_numpy(np.ascontiguousarray(k_static.T)).to(dev)       # (R, C), cells fastest
+    table = rate_law_table(ts1) if hasattr(ts1, "reactions") and hasattr(ts1, "props") else None
+    if table is not None:
+        # the rate constants of the first interval, on the device
+        k = device_rate_constants(ts1, cells.T, cells.P, params, dev, stream, table)
+    else:
+        # a mechanism object without reaction records: its own rate_constants
+        k_static = np.asarray(ts1.rate_constants(cells.T, cells.P, params), dtype=np.float64)
+        k = torch.from_numpy(np.ascontiguousarray(k_static.T)).to(dev)   # (R, C), cells fastest
     atol_d = torch.from_numpy(np.ascontiguousarray(atol_v)).to(dev)
     photo = _Photolysis(ts1, cells, photolysis, dev)
     step_list = list(range(-warmup_steps, nsteps))

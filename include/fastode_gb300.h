@@ -372,6 +372,42 @@ int fo_update_photolysis(int32_t C, int32_t nphoto, const int32_t* rxn, const do
                          const double* phase, double omega, double t, double* k,
                          int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
 
+/* Rate laws of a mechanism's reactions, evaluated per cell on the device
+ * (fastode.ts1.TS1.rate_constants, fastode/ts1.py:66-103), in the
+ * reference's operation order; T in K, P in Pa, M = P / (R T) in mol m^-3.
+ *   FO_RATE_ARRHENIUS  k = A exp(C / T) (T / D)^B (1 + E P);
+ *                      c = {A, B, C, D, E}
+ *   FO_RATE_TROE       k0 = A0 exp(C0 / T) (T / 300)^B0, kinf likewise,
+ *                      r = k0 M / kinf, k = k0 M / (1 + r) Fc^(N / (N + log10(r)^2));
+ *                      c = {A0, B0, C0, Ainf, Binf, Cinf, Fc, N}
+ *   FO_RATE_USER       k = param[column] * c[0] (the scaling factor)
+ *   FO_RATE_SURFACE    v = sqrt(c[0] T) with c[0] = 8 R / (pi mw),
+ *                      k = 4 n pi r^2 / (r / c[1] + 4 / (v c[2])), r the
+ *                      effective radius (param[column]), n the particle number
+ *                      concentration (param[column + 1]), c[1] the gas-phase
+ *                      diffusion coefficient, c[2] the reaction probability
+ * A scalar exponent of -1, 0, 0.5, 1 or 2 is evaluated as 1/x, 1, sqrt(x), x
+ * or x*x (as NumPy's array ** scalar does); others by pow. */
+#define FO_RATE_ARRHENIUS 0
+#define FO_RATE_TROE 1
+#define FO_RATE_USER 2
+#define FO_RATE_SURFACE 3
+
+typedef struct {
+  int32_t type;     /* FO_RATE_* */
+  int32_t column;   /* parameter column of FO_RATE_USER and FO_RATE_SURFACE, else -1 */
+  double c[8];      /* the law's constants, as above */
+} fo_rate_law;
+
+/* k[c, j] for R reactions and C cells: laws (R, device), T and P (C, device),
+ * params (device, column p of cell c at params[p * param_column_stride + c];
+ * may be NULL when no law reads a column), power (R, device; the third-body
+ * exponent, k *= M^power as fastode/ts1.py:100-102; NULL: none). The whole
+ * TS1 rate-constant builder on the device. Asynchronous on stream. */
+int fo_rate_laws(int32_t C, int32_t R, const fo_rate_law* laws, const double* T, const double* P,
+                 const double* params, int64_t param_column_stride, const double* power, double* k,
+                 int64_t k_cell_stride, int64_t k_reaction_stride, void* stream);
+
 /* Photolysis columns at an interval start from per-cell factors the caller
  * computed: k[c, rxn[p]] = J[p] * f[c], one correctly rounded product, which
  * is the assignment k[:, photo] = J[None, photo] * f[:, None] of a host rate

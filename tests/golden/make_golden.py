@@ -272,6 +272,29 @@ def backward_euler_ts1(reference):
     return out
 
 
+def ts1_rate_laws(reference):
+    """TS1's rate constants on the tier1-30s cells as the reference computes
+    them for the first interval of run_scenario (fastode/ts1.py:194-210: the
+    photolysis parameters scaled by the first scenario factor), with the
+    inputs the device evaluates them from: this package's law table compiled
+    from the reference's reaction records, the per-cell parameter columns,
+    T, P and the third-body powers."""
+    from fastode.ts1 import TS1, Cells, Scenario
+    from fastode_gb300.scenario import rate_law_table
+    ts1 = TS1()
+    sc = Scenario(Path(reference) / "data/scenarios/tier1-30s/scenario.txt")
+    cells = Cells(ts1, sc.cells)
+    f0 = sc.factor(0.0)
+    params = {k: (np.asarray(v) * f0 if k.startswith("j") else np.asarray(v)) for k, v in cells.params.items()}
+    k = ts1.rate_constants(cells.T, cells.P, params)
+    laws, columns = rate_law_table(ts1)
+    return dict(law_type=laws["type"], law_column=laws["column"], law_c=laws["c"],
+                params=np.stack([np.asarray(params[c], dtype=np.float64) for c in columns]),
+                columns=np.array(columns), T=np.asarray(cells.T, dtype=np.float64),
+                P=np.asarray(cells.P, dtype=np.float64),
+                power=np.asarray(ts1.mech.third_body_power, dtype=np.float64), k=k)
+
+
 SUBSET_INTERVALS = 30
 SUBSET_SNAPSHOTS = (10, 20, 30)
 
@@ -374,7 +397,7 @@ def c2_subset(reference):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["backward-euler", "c2-subset"], default=None,
+    ap.add_argument("--only", choices=["backward-euler", "c2-subset", "ts1-rate-laws"], default=None,
                     help="regenerate one fixture instead of all")
     a = ap.parse_args()
     sys.path.insert(0, a.reference)
@@ -385,6 +408,9 @@ def main():
     if a.only == "backward-euler":
         np.savez_compressed(HERE / "ts1_tier1_30s_backward_euler.npz", **backward_euler_ts1(a.reference))
         return
+    if a.only == "ts1-rate-laws":
+        np.savez_compressed(HERE / "ts1_rate_laws.npz", **ts1_rate_laws(a.reference))
+        return
     if a.only == "c2-subset":
         out = c2_subset(a.reference)
         np.savez_compressed(HERE / "ros3_210x500_subset.npz", **out)
@@ -393,6 +419,7 @@ def main():
         return
     out = c2_subset(a.reference)
     np.savez_compressed(HERE / "ros3_210x500_subset.npz", **out)
+    np.savez_compressed(HERE / "ts1_rate_laws.npz", **ts1_rate_laws(a.reference))
     np.savez_compressed(HERE / "ts1_tier1_30s_backward_euler.npz", **backward_euler_ts1(a.reference))
 
     ts1 = ts1_case(a.reference)

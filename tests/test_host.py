@@ -179,7 +179,7 @@ def test_struct_layouts_match_the_header(tmp_path):
         pytest.skip("no host C compiler")
     structs = {"fo_options": _abi.Options, "fo_batch_desc": _abi.BatchDesc,
                "fo_mechanism_desc": _abi.MechanismDesc, "fo_plan_info": _abi.PlanInfo,
-               "fo_gen_info": _abi.GenInfo}
+               "fo_gen_info": _abi.GenInfo, "fo_rate_law": _abi.RateLaw}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fastode_gb300.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
