@@ -37,14 +37,16 @@ sys.path.insert(0, str(ROOT))
 METRIC = "cell-intervals/s at rtol=1e-3 on 1 GB300 vs plain GPU + CPU ref; adjoint/forward cost"
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
-# FLOP of the integrator kernel (compact variant, refined ordering) on this
-# workload, from one ncu capture of the first two timed launches of
-# `bench.py --steps 2 --warmup 3 --no-cpu --e2e-steps 0 --plain-steps 0`
-# (3.590 TB over 0.799 PFLOP). The traffic of a launch is dominated by the
+# FLOP of the integrator kernel on this workload, by kernel variant, from ncu
+# captures (profiles/): the bench reports this ratio times its own FLOPs per
+# launch as `roofline.traffic`. compact: the first two timed launches of
+# `bench.py --kernel compact --steps 2 --warmup 3 --no-cpu --e2e-steps 0
+# --plain-steps 0` (3.590 TB over 0.799 PFLOP; the traffic is dominated by the
 # elimination's U operands, 8 bytes per 2-FLOP update, so it scales with the
-# algorithmic FLOPs; the bench reports this ratio times its own FLOPs per
-# launch.
-DRAM_BYTES_PER_FLOP = 4.491
+# FLOPs). A variant without a calibration reports no traffic.
+DRAM_BYTES_PER_FLOP = {"compact": 4.491}
+# the integrator kernel of each variant, as ncu names it
+KERNEL_NAME = {"generated": "fo_generated_solve_kernel"}
 
 
 # ---- CPU baseline: the oracle in a spawn pool, one group per worker --------------------
@@ -379,11 +381,16 @@ def run_ours(args, rank, world):
             "attempts": float(counts[:, 0].sum() / len(counts) / args.steps),
             "rejected": float(counts[:, 2].sum() / len(counts) / args.steps)},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": DRAM_BYTES_PER_FLOP * flops / args.steps,
+                     "frac": achieved / peak,
+                     "traffic": (DRAM_BYTES_PER_FLOP[args.kernel] * flops / args.steps
+                                 if args.kernel in DRAM_BYTES_PER_FLOP else None),
                      "traffic_unit": "bytes per launch",
-                     "traffic_source": "ncu DRAM bytes per algorithmic FLOP of this kernel on this workload "
-                                       f"({DRAM_BYTES_PER_FLOP} B/FLOP) times this run's FLOPs per launch",
-                     "kernel": "solve_kernel", "kernel_ms_per_launch": sum(solve_ms) / len(solve_ms),
+                     "traffic_source": (f"ncu DRAM bytes per algorithmic FLOP of this kernel on this workload "
+                                        f"({DRAM_BYTES_PER_FLOP[args.kernel]} B/FLOP) times this run's FLOPs "
+                                        "per launch" if args.kernel in DRAM_BYTES_PER_FLOP else
+                                        "not calibrated for this kernel variant"),
+                     "kernel": KERNEL_NAME.get(args.kernel, "solve_kernel"),
+                     "kernel_ms_per_launch": sum(solve_ms) / len(solve_ms),
                      "peak_source": "fo_fp64_fma_rate: full-warp DFMA kernel, same GPU, same run (the driver's "
                                     "peaks file holds HBM and bf16 only)",
                      "algorithmic_flops_per_launch": flops / args.steps},
@@ -499,7 +506,7 @@ def run_batched(args):
             "gpu_launches": args.steps * mb.launches_per_interval(), "parts": per_part, "clocks": clocks.summary(),
             "autotune": tuning,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": DRAM_BYTES_PER_FLOP * flops / args.steps,
+                         "frac": achieved / peak, "traffic": DRAM_BYTES_PER_FLOP["compact"] * flops / args.steps,
                          "traffic_unit": "bytes per interval (the 210/500 ratio; smaller mechanisms stream less)",
                          "time": "CUDA events around the graph replays of the timed intervals",
                          "peak_source": "fo_fp64_fma_rate, same GPU, same run"}}

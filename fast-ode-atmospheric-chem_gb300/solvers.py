@@ -125,7 +125,7 @@ class Algorithm:
     def __init__(self, tableau: Tableau = ROS3, controller: str = "h211b", b: float = 4.0,
                  safety: float = 0.9, fac_min: float = 0.2, fac_max: float = 6.0,
                  carry: bool = True, quantize: bool = True, max_steps: int = 1000,
-                 carry_memory: bool = True, ordering: str = "auto", kernel: str = "compact"):
+                 carry_memory: bool = True, ordering: str = "auto", kernel: str = "generated"):
         """The reference's arguments, plus two of the device path: the
         fill-reducing ``ordering`` of the sparse LU and the ``kernel`` variant:
         "generated", the mechanism's own factorization and solves generated as
@@ -189,7 +189,7 @@ class RestartingLoop(Algorithm):
     name = "restarting"
 
     def __init__(self, tableau: Tableau = ROS3, max_steps: int = 1000, step_change_rows: bool = True,
-                 ordering: str = "auto", kernel: str = "compact"):
+                 ordering: str = "auto", kernel: str = "generated"):
         super().__init__(tableau, controller="elementary", max_steps=max_steps, ordering=ordering, kernel=kernel)
         self.step_change_rows = step_change_rows
 
@@ -223,7 +223,7 @@ class BackwardEuler:
 
     def __init__(self, max_iterations: int = 11, reductions=(0.5, 0.5, 0.5, 0.5, 0.1),
                  small: float = 1.0e-40, max_steps: int = 1_000_000, ordering: str = "auto",
-                 kernel: str = "compact"):
+                 kernel: str = "generated"):
         self.max_iterations = max_iterations
         self.reductions = tuple(float(r) for r in reductions)
         if len(self.reductions) > 8:

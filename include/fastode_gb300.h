@@ -473,7 +473,7 @@ int fo_fp64_fma_rate(double* fma_per_second);
  * until the process exits, holding as many groups in flight as fit: one slot
  * per group in flight, of fo_workspace_bytes(plan, 2, C) -
  * fo_workspace_bytes(plan, 1, C) bytes (a 210-species / 500-reaction group of
- * 32 cells needs about 4.2 MB, so eight at a time); more groups than slots are
+ * 32 cells needs about 4.2 MB, so seven at a time); more groups than slots are
  * pulled from a device queue by the slots in turn. A mechanism whose single
  * group does not fit is rejected with FO_E_UNSUPPORTED. The first call on each
  * device looks up the array's device address and should come before any stream

@@ -39,7 +39,7 @@ def test_group_sizes_one_and_256_match_the_oracle(cuda, group_size):
 
 def _solve_call(torch, plan, ngroups, max_cells, Yd, kd, atol, dt, opts=None):
     from fastode_gb300 import Algorithm, _abi
-    opts = opts if opts is not None else Algorithm().options()
+    opts = opts if opts is not None else plan.options_for(Algorithm(), max(max_cells, 1))
     Cc = Yd.shape[1]
     offs = torch.tensor([0, Cc] if ngroups else [0], dtype=torch.int32, device="cuda")
     mem = torch.zeros((max(ngroups, 1), 3), dtype=torch.float64, device="cuda")

@@ -28,7 +28,7 @@ def test_static_scratch_matches_workspace_entry_point(cuda, case):
     offs = torch.from_numpy(group_offsets(Cc, 32)).cuda()
     G = len(offs) - 1
     atol = torch.from_numpy(f["atol"]).cuda()
-    opts = Algorithm().options()
+    opts = plan.options_for(Algorithm(), 32)     # the default (generated) variant
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
     def state():
@@ -74,7 +74,7 @@ def _tiled_subset(copies):
 
 
 def test_static_scratch_with_more_groups_than_slots(cuda):
-    """24 groups of the 210/500 mechanism against the eight slots that fit in
+    """24 groups of the 210/500 mechanism against the seven slots that fit in
     the static array: the slots take groups from the device queue in turn, and
     each reused slot still starts every group from its own inputs. Four
     intervals in a row (the controller memory of one interval feeds the next),
@@ -89,7 +89,7 @@ def test_static_scratch_with_more_groups_than_slots(cuda):
     slot = plan.workspace_bytes(2, 32) - plan.workspace_bytes(1, 32)
     lib = _abi.lib()
     atol = torch.from_numpy(f["atol"]).cuda()
-    opts = Algorithm().options()
+    opts = plan.options_for(Algorithm(), 32)     # the default (generated) variant
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
     def state(Yh):
