@@ -53,16 +53,20 @@ KERNEL_NAME = {"generated": "fo_generated_solve_kernel"}
 
 def _cpu_worker(args):
     """Integrate one group of the workload over `intervals` intervals with the
-    oracle; returns (cells, intervals, seconds)."""
+    reference (installed in baseline/_ref) or, without it, the oracle's
+    restatement; returns (cells, intervals, seconds, kind)."""
     group, n_cells, intervals = args
     os.environ["OMP_NUM_THREADS"] = os.environ["OPENBLAS_NUM_THREADS"] = "1"
     sys.path.insert(0, str(ROOT))
     from fastode_gb300 import synthetic as syn
-    from oracle import rosenbrock as O
+    from oracle.pool import group_solver
     wl = syn.plain_large(n_cells=n_cells, intervals=intervals).subset(slice(group * 32, group * 32 + 32))
+    kind, step, new_counts, new_memory = group_solver(wl)
+    Y, counts, mem = wl.cells.Y0.copy(), new_counts(), new_memory()
     t0 = time.perf_counter()
-    O.run_groups(wl.sm.mech, wl.cells.Y0, wl.k_at, wl.dt, intervals, wl.atol, wl.rtol)
-    return 32, intervals, time.perf_counter() - t0
+    for i in range(intervals):
+        Y, _ = step(Y, wl.k_at(i), counts, mem)
+    return 32, intervals, time.perf_counter() - t0, kind
 
 
 def cpu_baseline(n_cells, intervals, workers):
@@ -73,9 +77,10 @@ def cpu_baseline(n_cells, intervals, workers):
     with ctx.Pool(workers) as pool:
         res = pool.map(_cpu_worker, [(g, n_cells, intervals) for g in groups])
     wall = time.perf_counter() - t0
-    cell_int = sum(c * i for c, i, _ in res)
-    per_core = statistics.mean(c * i / s for c, i, s in res)
-    return cell_int / wall, per_core, wall
+    cell_int = sum(c * i for c, i, _, _ in res)
+    per_core = statistics.mean(c * i / s for c, i, s, _ in res)
+    kinds = {r[3] for r in res}
+    return cell_int / wall, per_core, wall, kinds.pop() if len(kinds) == 1 else "mixed"
 
 
 # ---- clocks during the timed region ----------------------------------------------------
@@ -406,8 +411,8 @@ def run_ours(args, rank, world):
     }
     if rank == 0 and args.cpu_intervals > 0 and not args.no_cpu:
         workers = args.cpu_workers or os.cpu_count()
-        thr, per_core, wall = cpu_baseline(args.cells, args.cpu_intervals, workers)
-        out["cpu_baseline"] = {"value": thr, "unit": "cell-intervals/s", "cores": workers, "kind": "port",
+        thr, per_core, wall, kind = cpu_baseline(args.cells, args.cpu_intervals, workers)
+        out["cpu_baseline"] = {"value": thr, "unit": "cell-intervals/s", "cores": workers, "kind": kind,
                                "per_core": per_core,
                                "sample": f"{workers} groups of 32 cells x the first {args.cpu_intervals} "
                                          f"intervals (cold start included), one group per process, "
@@ -670,14 +675,16 @@ def run_dae(args):
 
 
 def run_reference(args, rank, world):
-    """The reference's CPU path (the oracle port: the reference is Python and
-    does not travel) on every host core: each step advances one group per
+    """The reference's CPU path on every host core: the reference's own
+    Algorithm(ROS3).solve from its installation in baseline/_ref (the oracle's
+    restatement when it is not installed); each step advances one group per
     worker by one interval."""
     import multiprocessing as mp
     workers = args.cpu_workers or os.cpu_count()
     ctx = mp.get_context("spawn")
     from oracle.pool import GroupPool
     with GroupPool(ctx, workers, args.cells) as pool:
+        kind = pool.kind
         for i in range(args.warmup):
             pool.step()
         pool.reset()
@@ -692,9 +699,11 @@ def run_reference(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
         "config": {"workload": "ros3-210x500 (sample)", "cells": args.cells, "group_size": 32},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "cell-intervals/s", "cores": workers, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "cell-intervals/s", "cores": workers, "kind": kind,
                          "sample": f"{workers} groups of 32 cells (one per process), each step one interval "
-                                   f"of each, from the initial state"},
+                                   f"of each, from the initial state; "
+                                   + ("the unmodified reference installed in baseline/_ref" if kind == "reference"
+                                      else "the oracle's restatement of the reference")},
         "e2e": {"value": value, "unit": "cell-intervals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

@@ -7,7 +7,7 @@ one row per group (``COUNT_FIELDS`` gives the column order of that row).
 """
 from __future__ import annotations
 
-from dataclasses import dataclass, fields
+from dataclasses import dataclass
 
 COUNT_FIELDS = ("steps", "accepted", "rejected", "rhs", "jac", "lu", "solves", "newton",
                 "failures", "unconverged", "proj_passes", "proj_trials", "calls")
@@ -15,23 +15,32 @@ COUNT_FIELDS = ("steps", "accepted", "rejected", "rhs", "jac", "lu", "solves", "
 
 @dataclass
 class Counts:
-    steps: int = 0          # attempted steps (accepted + rejected)
+    """Thirteen integer counters, accumulated over calls. The three step
+    counters split every try of a step size into taken and retried; the next
+    four count the work each try costs (forcing evaluations, Jacobian
+    evaluations, factorizations of the stage matrix, and forward/backward
+    substitution pairs); the backward Euler loop alone moves the Newton
+    counters; the projection of constrained systems moves the two projection
+    counters; ``calls`` counts intervals."""
+
+    steps: int = 0
     accepted: int = 0
     rejected: int = 0
-    rhs: int = 0            # right-hand-side (forcing) evaluations
-    jac: int = 0            # Jacobian evaluations
-    lu: int = 0             # factorizations
-    solves: int = 0         # triangular-solve pairs
-    newton: int = 0         # Newton iterations (backward Euler)
-    failures: int = 0       # Newton convergence failures (backward Euler)
-    unconverged: int = 0    # unconverged iterates accepted (backward Euler)
-    proj_passes: int = 0    # projection passes (consistent initialization)
-    proj_trials: int = 0    # projection line-search trials
-    calls: int = 0          # solver calls (intervals)
+    rhs: int = 0
+    jac: int = 0
+    lu: int = 0
+    solves: int = 0
+    newton: int = 0
+    failures: int = 0
+    unconverged: int = 0
+    proj_passes: int = 0
+    proj_trials: int = 0
+    calls: int = 0
 
     def add(self, other: "Counts") -> None:
-        for f in fields(self):
-            setattr(self, f.name, getattr(self, f.name) + getattr(other, f.name))
+        """Accumulate another Counts field by field."""
+        for name in COUNT_FIELDS:
+            setattr(self, name, getattr(self, name) + getattr(other, name))
 
     def add_row(self, row) -> None:
         """Accumulate one device counts row (13 integers in COUNT_FIELDS order)."""
@@ -39,4 +48,5 @@ class Counts:
             setattr(self, name, getattr(self, name) + int(v))
 
     def as_dict(self) -> dict:
-        return {f.name: getattr(self, f.name) for f in fields(self)}
+        """The counters by name, in COUNT_FIELDS order."""
+        return dict(zip(COUNT_FIELDS, (getattr(self, name) for name in COUNT_FIELDS)))
