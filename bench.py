@@ -511,7 +511,9 @@ def run_batched(args):
             "gpu_launches": args.steps * mb.launches_per_interval(), "parts": per_part, "clocks": clocks.summary(),
             "autotune": tuning,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": DRAM_BYTES_PER_FLOP["compact"] * flops / args.steps,
+                         "frac": achieved / peak,
+                         "traffic": (DRAM_BYTES_PER_FLOP[kernel] * flops / args.steps
+                                     if kernel in DRAM_BYTES_PER_FLOP else None),
                          "traffic_unit": "bytes per interval (the 210/500 ratio; smaller mechanisms stream less)",
                          "time": "CUDA events around the graph replays of the timed intervals",
                          "peak_source": "fo_fp64_fma_rate, same GPU, same run"}}
@@ -544,18 +546,19 @@ def run_adjoint(args):
     target = forward([k * pert for k in ks]).Y.clone()
     forward(ks)                                                    # warm
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    fb = forward(ks)
-    torch.cuda.synchronize()
-    t_fwd = time.perf_counter() - t0
-    for rep in range(2):                                          # a warm-up pass, then the timed one
+    with Clocks(0) as clocks:
         t0 = time.perf_counter()
-        traj = A.forward_record(wl.sm.mech, wl.cells.Y0, lambda i: ks[i], wl.dt, wl.atol, wl.rtol, args.steps)
-        Y = traj.batch.Y
-        lam = 2.0 * (torch.log(Y + a) - torch.log(target + a)) / (Y + a)
-        lam0, thbar = A.adjoint(traj, lam)
+        fb = forward(ks)
         torch.cuda.synchronize()
-        t_fa = time.perf_counter() - t0
+        t_fwd = time.perf_counter() - t0
+        for rep in range(2):                                      # a warm-up pass, then the timed one
+            t0 = time.perf_counter()
+            traj = A.forward_record(wl.sm.mech, wl.cells.Y0, lambda i: ks[i], wl.dt, wl.atol, wl.rtol, args.steps)
+            Y = traj.batch.Y
+            lam = 2.0 * (torch.log(Y + a) - torch.log(target + a)) / (Y + a)
+            lam0, thbar = A.adjoint(traj, lam)
+            torch.cuda.synchronize()
+            t_fa = time.perf_counter() - t0
     g_th = thbar.sum(dim=1).cpu().numpy()
 
     def loss(Yend):
@@ -571,6 +574,9 @@ def run_adjoint(args):
         checks.append({"fd": fd, "adjoint": adj, "rel": abs(fd - adj) / max(abs(fd), 1e-300)})
     return {"metric": "adjoint/forward cost", "value": t_fa / t_fwd, "unit": "ratio", "higher_is_better": False,
             "forward_s": t_fwd, "forward_plus_adjoint_s": t_fa, "max_steps_per_interval": traj.max_steps,
+            "clocks": clocks.summary(), "kernel": traj.batch.alg.kernel,
+            "time": "wall clock around the forward run and around the recording forward plus the adjoint "
+                    "(both synchronized), the second of two passes",
             "config": {"workload": f"adjoint ROS3 210x500, {args.cells} cells, {args.steps} x 30 s, "
                                    "gradients w.r.t. 500 log rate constants and the initial state"},
             "fd_checks": checks,
@@ -674,6 +680,36 @@ def run_dae(args):
     return out
 
 
+def run_extras(args):
+    """The rest of the metric, measured in the same run on the same GPU: the
+    batched uneven workload (1,048,576 cells over three mechanisms, one
+    persistent launch per interval replayed as a CUDA graph), the adjoint cost
+    of the 210/500 mechanism (4,096 cells, 60 intervals) and the constrained
+    RODAS3 workload with its adjoint cost. Each entry is its own bench line
+    (value, clocks, roofline where it has one); a failure is reported in
+    place of the entry."""
+    import gc
+    from types import SimpleNamespace
+    import torch
+    extras = {}
+    runs = {
+        "batched": (run_batched, dict(cells=1048576, steps=3, warmup=3, kernel=args.kernel, ordering=args.ordering,
+                                      autotune=False)),
+        "adjoint": (run_adjoint, dict(cells=4096, steps=60, fd_directions=4)),
+        "dae": (run_dae, dict(cells=16384, steps=30, warmup=3, adjoint_intervals=5, fd_directions=4)),
+    }
+    for name, (fn, kw) in runs.items():
+        gc.collect()
+        torch.cuda.empty_cache()
+        t0 = time.perf_counter()
+        try:
+            extras[name] = fn(SimpleNamespace(**kw))
+        except Exception as e:                       # report, keep the headline line
+            extras[name] = {"error": f"{type(e).__name__}: {e}"}
+        extras[name]["wall_s"] = time.perf_counter() - t0
+    return extras
+
+
 def run_reference(args, rank, world):
     """The reference's CPU path on every host core: the reference's own
     Algorithm(ROS3).solve from its installation in baseline/_ref (the oracle's
@@ -737,6 +773,9 @@ def main():
                     help="central-difference directions checking the adjoint gradient")
     ap.add_argument("--adjoint-intervals", type=int, default=0,
                     help="dae workload: intervals of the adjoint cost measurement (0: none)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="plain workload: skip the batched, adjoint and constrained measurements that the "
+                         "default run adds to its line")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -754,6 +793,8 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     out = run_ours(args, rank, world)
+    if rank == 0 and world == 1 and not args.no_extras:
+        out.update(run_extras(args))
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

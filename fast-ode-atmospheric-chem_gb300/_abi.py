@@ -124,7 +124,7 @@ SIGNATURES = {
     "fo_adjoint_workspace_bytes": (C.c_int, [_P, _I32, _I32, _I32, C.POINTER(C.c_size_t)]),
     "fo_adjoint_interval": (C.c_int, [_P, C.POINTER(Options), _I32, _P, _I32,
                                       _P, _I64, _I64, _P, _I64, _I64, _P, _D,
-                                      _P, _P, _I32, _I32,
+                                      _P, _P, _I32, _P, _P, _I32,
                                       _P, _I64, _I64, _P, _I64, _I64, _P, _I64, _I64,
                                       _P, _P, C.c_size_t, _P]),
 }

@@ -3,8 +3,10 @@
 The reference has no sensitivities; this is new. A forward run over many
 intervals records, per interval, the state at its start (a checkpoint), its
 rate constants and every group's accepted step sizes (from the device trace).
-With those step sizes held fixed, each interval is a smooth map of its start
-state and the log rate constants through the Rosenbrock steps and the clamp;
+With those step sizes held fixed (and, for constrained systems, the line-search
+steps of the projection's Newton updates that start each call), each interval
+is a smooth map of its start state and the log rate constants through the
+projection, the Rosenbrock steps and the clamp;
 ``adjoint`` walks the intervals backwards, and the device kernel
 (``fo_adjoint_interval``) replays each interval from its checkpoint and runs
 the reverse stage sweep with transposed solves on the same factorizations and
@@ -36,6 +38,8 @@ class Trajectory:
     step_ptr: list              # per interval: (G+1,) int32 device
     steps: list                 # per interval: flat accepted step sizes, device
     max_steps: int
+    proj_ptr: list              # per interval: (G+1,) int32 device, or None (no algebraic species)
+    proj_steps: list            # per interval: flat line-search steps of the projection's updates
     dt: float
     atol: object                # (n,) device
     statuses: list              # per interval: statuses after the forward call
@@ -51,8 +55,9 @@ def forward_record(mech, Y0, k_of, dt, atol, rtol, intervals, group_size=32, alg
     b = Batch(mech, Y0, group_size=group_size, algorithm=alg, mass=mass, trace_cap=trace_cap)
     at = atol if isinstance(atol, torch.Tensor) else torch.from_numpy(
         np.array(np.broadcast_to(np.asarray(atol, dtype=np.float64), (b.plan.n,)))).to(b.Y.device)
-    cps, ks, ptrs, steps, sts = [], [], [], [], []
+    cps, ks, ptrs, steps, sts, pptrs, psteps = [], [], [], [], [], [], []
     max_steps = 1
+    constrained = b.plan.has_constraints
     for i in range(intervals):
         k = k_of(i)
         cps.append(b.Y.clone())
@@ -62,18 +67,30 @@ def forward_record(mech, Y0, k_of, dt, atol, rtol, intervals, group_size=32, alg
         if np.any(tl > trace_cap):
             raise RuntimeError(f"interval {i}: more than {trace_cap} attempts in a group; raise trace_cap")
         tr = b.trace.cpu().numpy()
-        ptr = [0]
-        flat = []
+        status = b.statuses()
+        ptr, pptr = [0], [0]
+        flat, pflat = [], []
         for g in range(b.ngroups):
             rec = tr[g, : tl[g]]
             acc = rec[rec[:, 3] == 1.0, 1]
             flat.extend(acc.tolist())
             ptr.append(len(flat))
             max_steps = max(max_steps, len(acc))
+            # the projection's accepted updates; a failed projection restores
+            # the state, so none of its updates remain
+            if status[g] != "projection failed":
+                pflat.extend(rec[rec[:, 3] == 2.0, 1].tolist())
+            pptr.append(len(pflat))
         ptrs.append(torch.tensor(ptr, dtype=torch.int32, device=b.Y.device))
         steps.append(torch.tensor(flat if flat else [0.0], dtype=torch.float64, device=b.Y.device))
-        sts.append(b.statuses())
-    return Trajectory(b, cps, ks, ptrs, steps, max_steps, float(dt), at, sts)
+        if constrained:
+            pptrs.append(torch.tensor(pptr, dtype=torch.int32, device=b.Y.device))
+            psteps.append(torch.tensor(pflat if pflat else [0.0], dtype=torch.float64, device=b.Y.device))
+        else:
+            pptrs.append(None)
+            psteps.append(None)
+        sts.append(status)
+    return Trajectory(b, cps, ks, ptrs, steps, max_steps, pptrs, psteps, float(dt), at, sts)
 
 
 def _workspace(traj: Trajectory):
@@ -95,7 +112,9 @@ def _call(traj, i, mode, ws, Yin, lam=None, thbar=None, Yout=None, k=None):
     rc = _abi.lib().fo_adjoint_interval(
         b.plan.handle, C.byref(b.opts), b.ngroups, b.offsets.data_ptr(), b.max_cells,
         Yin.data_ptr(), 1, Cc, k.data_ptr(), 1, Cc, traj.atol.data_ptr(), traj.dt,
-        traj.step_ptr[i].data_ptr(), traj.steps[i].data_ptr(), traj.max_steps, mode,
+        traj.step_ptr[i].data_ptr(), traj.steps[i].data_ptr(), traj.max_steps,
+        traj.proj_ptr[i].data_ptr() if traj.proj_ptr[i] is not None else None,
+        traj.proj_steps[i].data_ptr() if traj.proj_steps[i] is not None else None, mode,
         lam.data_ptr() if lam is not None else None, 1, Cc,
         thbar.data_ptr() if thbar is not None else None, 1, Cc,
         Yout.data_ptr() if Yout is not None else None, 1, Cc,

@@ -305,7 +305,7 @@ int fo_plan_generate(fo_plan* plan, const char* cache_dir, fo_gen_info* info) {
   if (!plan->gen) {
     std::string err;
     fo_gen_info gi;
-    int rc = fo::gen_create(plan->host, cache_dir, &plan->gen, &gi, &err);
+    int rc = fo::gen_create({&plan->host}, cache_dir, &plan->gen, &gi, &err);
     if (rc != FO_OK) return fail(rc, err);
     plan->gen_info = gi;
   }
@@ -338,11 +338,8 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
       opt->variant != FO_VARIANT_GENERATED)
     return fail(FO_E_INVALID, "unknown kernel variant");
   int variant = opt->variant;
-  if (variant == FO_VARIANT_GENERATED) {
-    if (!plan->gen) return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED needs fo_plan_generate on this plan first");
-    if (max_group_cells <= 0 || max_group_cells > 32)
-      return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED runs groups of at most 32 cells");
-  }
+  if (variant == FO_VARIANT_GENERATED && (max_group_cells <= 0 || max_group_cells > 32))
+    return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED runs groups of at most 32 cells");
   if (variant == FO_VARIANT_COMPACT && plan->dev.cep == nullptr) variant = FO_VARIANT_PIPELINED;
   if (variant == FO_VARIANT_PIPELINED && plan->dev.elp == nullptr) variant = FO_VARIANT_PLAIN;
   if (max_group_cells <= 0 || max_group_cells > kMaxLanes)
@@ -418,6 +415,7 @@ int fill_params(const fo_plan* plan, const fo_options* opt, int32_t ngroups, con
 struct fo_multi {
   int nb = 0, grid = 0, lanes = 0;
   size_t smem = 0;
+  fo::GenModule* gen = nullptr;          // the generated module of every batch's mechanism
   fo::SolveParams* d_batches = nullptr;  // in the workspace
   int32_t* d_starts = nullptr;
   int32_t* d_queue = nullptr;
@@ -463,6 +461,8 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
              int32_t slots, double* trace, int32_t trace_cap, int32_t* trace_len, void* stream) {
   if (!workspace) return fail(FO_E_INVALID, "null workspace");
   if (ngroups <= 0) return FO_OK;
+  if (opt && opt->variant == FO_VARIANT_GENERATED && plan && !plan->gen)
+    return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED needs fo_plan_generate on this plan first");
   fo::SolveParams p;
   size_t smem = 0;
   int rc = fill_params(plan, opt, ngroups, group_offsets, max_group_cells, Y, y_cell_stride, y_species_stride, k,
@@ -524,10 +524,26 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
                      d.y_species_stride, d.k, d.k_cell_stride, d.k_reaction_stride, d.atol, d.rtol, d.dt, d.memory,
                      d.counts, d.status, &params[j], &sm);
     if (rc != FO_OK) return rc;
-    if (params[j].o.variant == FO_VARIANT_GENERATED)
-      return fail(FO_E_UNSUPPORTED, "the several-mechanism launch runs the table-driven variants");
-    smem = std::max(smem, smem_bytes(d.plan->host, L.lanes, params[j].o.variant));
+    smem = std::max(smem, params[j].o.variant == FO_VARIANT_GENERATED ? sm
+                                                                       : smem_bytes(d.plan->host, L.lanes,
+                                                                                    params[j].o.variant));
     starts[j + 1] = starts[j] + d.ngroups;
+  }
+  // the generated variant: one module with every distinct mechanism, each
+  // batch pointing at its own by index (all batches generated, or none)
+  int ngen = 0;
+  for (const auto& p : params) ngen += p.o.variant == FO_VARIANT_GENERATED ? 1 : 0;
+  if (ngen != 0 && ngen != nb)
+    return fail(FO_E_UNSUPPORTED, "one launch runs either the generated variant for every batch or for none");
+  std::vector<const fo::HostTables*> tables;
+  if (ngen) {
+    if (L.lanes != 32) return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED runs groups of at most 32 cells");
+    for (int j = 0; j < nb; ++j) {
+      const fo::HostTables* t = &b[order[j]].plan->host;
+      auto it = std::find(tables.begin(), tables.end(), t);
+      params[j].o.gen_index = (int)(it - tables.begin());
+      if (it == tables.end()) tables.push_back(t);
+    }
   }
   int dev = 0, smem_max = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -538,6 +554,14 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
   char* ws = static_cast<char*>(workspace);
   fo_multi* m = new (std::nothrow) fo_multi;
   if (!m) return fail(FO_E_ALLOC, "host allocation failed");
+  if (ngen) {
+    std::string err;
+    rc = fo::gen_create(tables, nullptr, &m->gen, nullptr, &err);
+    if (rc != FO_OK) {
+      delete m;
+      return fail(rc, err);
+    }
+  }
   m->nb = nb;
   m->grid = L.grid;
   m->lanes = L.lanes;
@@ -557,6 +581,7 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
   if (e == cudaSuccess)
     e = cudaMemcpy(m->d_starts, starts.data(), sizeof(int32_t) * (nb + 1), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
+    fo::gen_destroy(m->gen);
     delete m;
     return cuda_fail(e, "cudaMemcpy(batch table)");
   }
@@ -566,14 +591,18 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
 
 int fo_multi_launch(const fo_multi* m, void* stream) {
   if (!m) return fail(FO_E_INVALID, "null argument");
-  cudaError_t e = fo::launch_solve_multi(m->d_batches, m->nb, m->d_starts, m->d_queue, m->d_scratch,
-                                         m->slot_doubles, m->grid, m->lanes, m->smem,
-                                         static_cast<cudaStream_t>(stream));
+  cudaError_t e = m->gen ? fo::gen_launch_multi(m->gen, m->d_batches, m->nb, m->d_starts, m->d_queue,
+                                                m->d_scratch, m->slot_doubles, m->grid, m->smem,
+                                                static_cast<cudaStream_t>(stream))
+                         : fo::launch_solve_multi(m->d_batches, m->nb, m->d_starts, m->d_queue, m->d_scratch,
+                                                  m->slot_doubles, m->grid, m->lanes, m->smem,
+                                                  static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "multi solve launch");
   return FO_OK;
 }
 
 int fo_multi_destroy(fo_multi* m) {
+  if (m) fo::gen_destroy(m->gen);
   delete m;
   return FO_OK;
 }
@@ -593,6 +622,11 @@ fo::AdjLayout adjoint_layout(const fo::HostTables& t, int max_steps) {
   a.g = o; o += t.n;
   a.jbar = o; o += (int64_t)t.j_col.size();
   a.dbar = o; o += (int64_t)t.R * t.P;
+  bool constrained = false;
+  for (double m : t.mass) constrained = constrained || m == 0.0;
+  a.yp = o; o += constrained ? (int64_t)fo::kMaxProjectionUpdates * t.n : 0;
+  a.pdelta = o; o += constrained ? t.n : 0;
+  a.pmu = o; o += constrained ? t.n : 0;
   a.items = o;
   return a;
 }
@@ -613,7 +647,8 @@ int fo_adjoint_workspace_bytes(const fo_plan* plan, int32_t ngroups, int32_t max
 int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const int32_t* group_offsets,
                         int32_t max_group_cells, const double* Y, int64_t ycs, int64_t yss, const double* k,
                         int64_t kcs, int64_t krs, const double* atol, double dt, const int32_t* step_ptr,
-                        const double* steps, int32_t max_steps, int32_t mode, double* lam, int64_t lcs, int64_t lss,
+                        const double* steps, int32_t max_steps, const int32_t* proj_ptr, const double* proj_steps,
+                        int32_t mode, double* lam, int64_t lcs, int64_t lss,
                         double* thbar, int64_t tcs, int64_t trs, double* Yout, int64_t ocs, int64_t oss,
                         int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
   if (ngroups <= 0) return FO_OK;
@@ -635,8 +670,13 @@ int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngro
   fo_adjoint_workspace_bytes(plan, ngroups, max_group_cells, max_steps, &need);
   if (workspace_bytes < need) return fail(FO_E_WORKSPACE, "workspace too small");
   a.al = adjoint_layout(plan->host, max_steps);
-  if (a.p.o.variant == FO_VARIANT_COMPACT || a.p.o.variant == FO_VARIANT_GENERATED) {
-    // the transposed solves need the whole vector on chip
+  const bool generated = a.p.o.variant == FO_VARIANT_GENERATED && plan->gen != nullptr;
+  if (generated) {
+    // the generated adjoint keeps nothing else on chip but the projection's
+    // dense work row (constrained mechanisms)
+    smem = sizeof(double) * (32 + (plan->dev.has_constraints ? (size_t)plan->host.n * a.p.lanes : 0));
+  } else if (a.p.o.variant == FO_VARIANT_COMPACT || a.p.o.variant == FO_VARIANT_GENERATED) {
+    // the table-driven transposed solves need the whole vector on chip
     a.p.o.variant = plan->dev.elp ? FO_VARIANT_PIPELINED : FO_VARIANT_PLAIN;
     smem = smem_bytes(plan->host, a.p.lanes, a.p.o.variant);
   }
@@ -656,10 +696,17 @@ int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngro
   a.oss = oss;
   a.step_ptr = step_ptr;
   a.steps = steps;
+  if ((proj_ptr == nullptr) != (proj_steps == nullptr))
+    return fail(FO_E_INVALID, "proj_ptr and proj_steps go together");
+  if (proj_ptr && !plan->dev.has_constraints)
+    return fail(FO_E_INVALID, "projection updates given for a mechanism without algebraic species");
+  a.proj_ptr = proj_ptr;
+  a.proj_steps = proj_steps;
   a.max_steps = max_steps;
   a.mode = mode;
   a.status = status;
-  cudaError_t e = fo::launch_adjoint(a, ngroups, a.p.lanes, smem, static_cast<cudaStream_t>(stream));
+  cudaError_t e = generated ? fo::gen_launch_adjoint(plan->gen, a, ngroups, smem, static_cast<cudaStream_t>(stream))
+                            : fo::launch_adjoint(a, ngroups, a.p.lanes, smem, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
   return FO_OK;
 }

@@ -24,7 +24,8 @@
 // The solves: blocks of `solve_block` rows; each row sums its terms in
 // ascending column order, as the plain variant's loops do, so results match
 // that variant bit for bit; a solution value used by several rows of a block
-// is loaded once for the block.
+// is loaded once for the block. The transposed solve of the adjoint follows
+// the same pattern with rows and columns exchanged.
 #include "codegen.h"
 
 #include <algorithm>
@@ -287,43 +288,133 @@ void emit_solve(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Patt
   }
 }
 
-std::string function(const char* name, const char* params, const Ptx& x, const char* prologue) {
+// The transposed solve A^T x = b in place on the solve vector, the gather
+// form of the adjoint's scatter loops (U^T z = b by rows ascending, then
+// L^T x = z by rows descending): entry c receives fma(-U(r, c), z_r, .) for
+// r ascending, then z_c = . * (1 / pivot_c); later fma(-L(r, c), x_r, .) for r
+// descending; the operations of the table-driven kernel in its order.
+void emit_solve_t(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pattern& P, int b) {
+  const int n = t.n;
+  const int nb = (n + b - 1) / b;
+  std::vector<int> xv(n, -1);
+  // U^T z = b, columns of U ascending
+  for (int ib = 0; ib < nb; ++ib) {
+    const int c0 = ib * b, c1 = std::min(n, c0 + b);
+    std::vector<int> acc(b);
+    for (int c = c0; c < c1; ++c) acc[c - c0] = x.load(sl.xs + c);
+    for (int r = 0; r < c0; ++r) {
+      int zr = -1;
+      for (int c = c0; c < c1; ++c) {
+        const int q = P.at(r, c);
+        if (q < 0) continue;
+        if (zr < 0) zr = x.load(sl.xs + r);
+        acc[c - c0] = x.fma(x.neg(x.load(sl.lu + q)), zr, acc[c - c0]);
+      }
+    }
+    for (int c = c0; c < c1; ++c) {
+      for (int r = c0; r < c; ++r) {
+        const int q = P.at(r, c);
+        if (q >= 0) acc[c - c0] = x.fma(x.neg(x.load(sl.lu + q)), xv[r], acc[c - c0]);
+      }
+      xv[c] = x.mul(acc[c - c0], x.load(sl.lu + P.at(c, c)));
+      x.store(sl.xs + c, xv[c]);
+    }
+  }
+  // L^T x = z, columns of L descending
+  for (int ib = nb - 1; ib >= 0; --ib) {
+    const int c0 = ib * b, c1 = std::min(n, c0 + b);
+    std::vector<int> acc(b);
+    for (int c = c0; c < c1; ++c) acc[c - c0] = x.load(sl.xs + c);
+    for (int r = n - 1; r >= c1; --r) {
+      int xr = -1;
+      for (int c = c0; c < c1; ++c) {
+        const int q = P.at(r, c);
+        if (q < 0) continue;
+        if (xr < 0) xr = x.load(sl.xs + r);
+        acc[c - c0] = x.fma(x.neg(x.load(sl.lu + q)), xr, acc[c - c0]);
+      }
+    }
+    for (int c = c1 - 1; c >= c0; --c) {
+      for (int r = c1 - 1; r > c; --r) {
+        const int q = P.at(r, c);
+        if (q >= 0) acc[c - c0] = x.fma(x.neg(x.load(sl.lu + q)), acc[r - c0], acc[c - c0]);
+      }
+      x.store(sl.xs + c, acc[c - c0]);
+    }
+  }
+}
+
+// One function whose body dispatches on the mechanism index parameter %m
+// to the mechanism's code (`bodies[i]`, all numbered in one register space).
+std::string function(const char* name, const char* params, const Ptx& x, const std::vector<std::string>& bodies,
+                     const char* prologue) {
   std::string s;
-  s.reserve(x.body.size() + 512);
+  size_t total = 0;
+  for (const auto& b : bodies) total += b.size();
+  s.reserve(total + 1024);
   s += ".visible .func ";
   s += name;
   s += "(";
   s += params;
   s += ")\n{\n\t.reg .f64 %d<" + std::to_string(x.next + 1) + ">;\n\t.reg .b64 %p;\n\t.reg .b64 %b;\n"
-       "\t.reg .b64 %a;\n";
+       "\t.reg .b64 %a;\n\t.reg .b32 %m;\n\t.reg .pred %q;\n";
   s += prologue;
-  s += x.body;
-  s += "\tret;\n}\n";
+  for (size_t i = 0; i < bodies.size(); ++i) {
+    const std::string label = std::string("$") + name + "_m" + std::to_string(i + 1);
+    if (i + 1 < bodies.size()) s += "\tsetp.ne.s32 %q, %m, " + std::to_string(i) + ";\n\t@%q bra " + label + ";\n";
+    s += bodies[i];
+    s += "\tret;\n";
+    if (i + 1 < bodies.size()) s += label + ":\n";
+  }
+  s += "}\n";
   return s;
 }
 
 }  // namespace
 
-std::string generate_ptx(const HostTables& t, const GenOptions& o, int64_t* fma_count) {
+std::string generate_ptx(const std::vector<const HostTables*>& ts, const GenOptions& o, int64_t* fma_count) {
   if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64)
     throw std::invalid_argument("tile sizes out of range");
-  const ScratchLayout sl = layout_of(t);
-  const Pattern P = pattern_of(t);
-  Ptx f;
-  int64_t nfma = 0;
-  emit_factor(f, t, sl, P, o.tile, &nfma);
-  if (nfma != t.lu_fma) throw std::logic_error("generated factorization does not match the symbolic count");
-  if (fma_count) *fma_count = nfma;
-  Ptx s;
-  emit_solve(s, t, sl, P, o.solve_block);
+  if (ts.empty()) throw std::invalid_argument("no mechanism");
+  Ptx f, s, st;
+  std::vector<std::string> fb, sb, tb;
+  int64_t total = 0;
+  for (const HostTables* t : ts) {
+    const ScratchLayout sl = layout_of(*t);
+    const Pattern P = pattern_of(*t);
+    int64_t nfma = 0;
+    emit_factor(f, *t, sl, P, o.tile, &nfma);
+    if (nfma != t->lu_fma) throw std::logic_error("generated factorization does not match the symbolic count");
+    total += nfma;
+    fb.push_back(std::move(f.body));
+    f.body.clear();
+    emit_solve(s, *t, sl, P, o.solve_block);
+    sb.push_back(std::move(s.body));
+    s.body.clear();
+    emit_solve_t(st, *t, sl, P, o.solve_block);
+    tb.push_back(std::move(st.body));
+    st.body.clear();
+  }
+  if (fma_count) *fma_count = total;
   std::string out = ".version 9.0\n.target sm_103a\n.address_size 64\n\n";
-  out += function("fo_gen_factor", ".param .b64 fo_gen_factor_base, .param .b64 fo_gen_factor_alpha", f,
+  out += function("fo_gen_factor",
+                  ".param .b64 fo_gen_factor_base, .param .b64 fo_gen_factor_alpha, .param .b32 fo_gen_factor_mech",
+                  f, fb,
                   "\tld.param.b64 %p, [fo_gen_factor_base];\n\tld.param.b64 %a, [fo_gen_factor_alpha];\n"
-                  "\tmov.b64 %d0, %a;\n\tcvta.to.global.u64 %b, %p;\n");
+                  "\tld.param.b32 %m, [fo_gen_factor_mech];\n\tmov.b64 %d0, %a;\n\tcvta.to.global.u64 %b, %p;\n");
   out += "\n";
-  out += function("fo_gen_solve", ".param .b64 fo_gen_solve_base", s,
-                  "\tld.param.b64 %p, [fo_gen_solve_base];\n\tcvta.to.global.u64 %b, %p;\n");
+  out += function("fo_gen_solve", ".param .b64 fo_gen_solve_base, .param .b32 fo_gen_solve_mech", s, sb,
+                  "\tld.param.b64 %p, [fo_gen_solve_base];\n\tld.param.b32 %m, [fo_gen_solve_mech];\n"
+                  "\tcvta.to.global.u64 %b, %p;\n");
+  out += "\n";
+  out += function("fo_gen_solve_t", ".param .b64 fo_gen_solve_t_base, .param .b32 fo_gen_solve_t_mech", st, tb,
+                  "\tld.param.b64 %p, [fo_gen_solve_t_base];\n\tld.param.b32 %m, [fo_gen_solve_t_mech];\n"
+                  "\tcvta.to.global.u64 %b, %p;\n");
   return out;
+}
+
+std::string generate_ptx(const HostTables& t, const GenOptions& o, int64_t* fma_count) {
+  return generate_ptx(std::vector<const HostTables*>{&t}, o, fma_count);
 }
 
 }  // namespace fo

@@ -67,6 +67,7 @@ struct DevOptions {
   double b, safety, fac_min, fac_max;
   int carry, quantize, carry_memory, max_steps;
   int variant;     // FO_VARIANT_*
+  int gen_index;   // FO_VARIANT_GENERATED: the mechanism's index in its generated module
   int loop;        // FO_LOOP_*
   int step_change_rows;
   double k_exp;    // embedded order + 1
@@ -117,8 +118,15 @@ struct AdjLayout {
   int64_t g;      // n: a forcing vector-Jacobian product
   int64_t jbar;   // nnzj
   int64_t dbar;   // R*P
+  int64_t yp;     // constrained systems: kMaxProjectionUpdates * n, the state before each projection update
+  int64_t pdelta; // n: a projection update's Newton correction
+  int64_t pmu;    // n: its adjoint
   int64_t items;  // total items per lane, forward layout included
 };
+
+// The projection's update limit (fastode/solvers.py:100-178: ten updates and
+// the check after them), the most updates one call can apply.
+constexpr int kMaxProjectionUpdates = 11;
 
 struct AdjParams {
   SolveParams p;        // tables, tableau, forward scratch layout, rate constants, group offsets, dt
@@ -134,6 +142,8 @@ struct AdjParams {
   const int32_t* step_ptr;  // ngroups+1
   const double* steps;      // accepted step sizes of the interval
   int max_steps;
+  const int32_t* proj_ptr;  // ngroups+1, or null: the projection updates of each group
+  const double* proj_steps; // their accepted line-search steps
   int mode;             // 0 replay, 1 adjoint
   int32_t* status;
 };

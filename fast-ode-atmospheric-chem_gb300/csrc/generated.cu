@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include "adjoint.cuh"
 #include "rosenbrock.cuh"
 
 extern "C" __global__ void __launch_bounds__(32, 16) fo_generated_solve_kernel(fo::SolveParams p) {
@@ -36,4 +37,36 @@ extern "C" __global__ void __launch_bounds__(32, 16) fo_generated_solve_kernel(f
     if (g >= p.ngroups) break;
     fo::solve_group(p, g, scr, w, red);
   }
+}
+
+// Several mechanisms in one persistent launch (the generated form of
+// solve_multi_kernel): items [starts[b], starts[b+1]) of the queue are the
+// groups of batch b, whose parameters carry the mechanism's index in this
+// module; each block integrates whatever group it pulls next.
+extern "C" __global__ void __launch_bounds__(32, 16)
+    fo_generated_multi_kernel(const fo::SolveParams* __restrict__ batches, int nb, const int32_t* __restrict__ starts,
+                              int32_t* queue, double* scratch, int64_t slot_doubles) {
+  extern __shared__ double smem[];
+  double* red = smem;
+  double* w = smem + 32;
+  double* scr = scratch + (int64_t)blockIdx.x * slot_doubles;
+  __shared__ int next;
+  const int total = starts[nb];
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) next = atomicAdd(queue, 1);
+    __syncthreads();
+    const int item = next;
+    if (item >= total) break;
+    int b = 0;
+    while (b + 1 < nb && item >= starts[b + 1]) ++b;
+    fo::solve_group(batches[b], item - starts[b], scr, w, red);
+  }
+}
+
+// The discrete adjoint of one interval (adjoint.cuh) on the mechanism's
+// generated factorization, solves and transposed solves.
+extern "C" __global__ void __launch_bounds__(32, 16) fo_generated_adjoint_kernel(fo::AdjParams a) {
+  extern __shared__ double smem[];
+  fo::adjoint_group(a, smem + 32);
 }

@@ -23,9 +23,8 @@
 // values use FMA.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "rosenbrock.cuh"
+#include "smem_attribute.h"
 
 namespace fo {
 
@@ -85,33 +84,6 @@ __global__ void eval_kernel(SolveParams p, int C, int want_jac, double* out) {
 #undef WROW
 
 // ---- launch wrappers ----------------------------------------------------------
-
-// The dynamic shared-memory limit above 48 KB is an attribute of a kernel on
-// one device: it is set once per (kernel, device) for the largest size asked
-// so far, under a lock, so a process that drives several devices, or several
-// host threads, never launches on a device where it was not set.
-class SmemAttribute {
- public:
-  explicit SmemAttribute(const void* kernel) : kernel_(kernel) {}
-  cudaError_t ensure(size_t smem) {
-    if (smem <= 48 * 1024) return cudaSuccess;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(mutex_);
-    if ((int)smem <= configured_[dev]) return cudaSuccess;
-    e = cudaFuncSetAttribute(kernel_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) configured_[dev] = (int)smem;
-    return e;
-  }
-
- private:
-  static constexpr int kMaxDevices = 64;
-  const void* kernel_;
-  std::mutex mutex_;
-  int configured_[kMaxDevices] = {};
-};
 
 cudaError_t launch_solve(const SolveParams& p, int grid, size_t smem, cudaStream_t stream) {
   static SmemAttribute attribute(reinterpret_cast<const void*>(solve_kernel));

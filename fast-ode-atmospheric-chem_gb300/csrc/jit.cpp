@@ -182,18 +182,21 @@ bool link(const std::string& ptx, std::vector<char>* cubin, std::string* err) {
 
 struct GenModule {
   cudaLibrary_t lib = nullptr;
-  cudaKernel_t kernel = nullptr;
+  cudaKernel_t kernel = nullptr;        // fo_generated_solve_kernel
+  cudaKernel_t multi_kernel = nullptr;  // fo_generated_multi_kernel
+  cudaKernel_t adjoint_kernel = nullptr;  // fo_generated_adjoint_kernel
   std::mutex mutex;
-  int configured_smem[64] = {};
+  int configured_smem[3][64] = {};
 };
 
-int gen_create(const HostTables& t, const char* cache_dir, GenModule** out, fo_gen_info* info, std::string* err) {
+int gen_create(const std::vector<const HostTables*>& ts, const char* cache_dir, GenModule** out, fo_gen_info* info,
+               std::string* err) {
   const auto t0 = std::chrono::steady_clock::now();
   *out = nullptr;
   GenOptions opt;
   std::string ptx;
   try {
-    ptx = generate_ptx(t, opt);
+    ptx = generate_ptx(ts, opt);
   } catch (const std::exception& e) {
     *err = std::string("code generation failed: ") + e.what();
     return FO_E_INVALID;
@@ -220,6 +223,8 @@ int gen_create(const HostTables& t, const char* cache_dir, GenModule** out, fo_g
   GenModule* m = new GenModule;
   cudaError_t e = cudaLibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->kernel, m->lib, "fo_generated_solve_kernel");
+  if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->multi_kernel, m->lib, "fo_generated_multi_kernel");
+  if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->adjoint_kernel, m->lib, "fo_generated_adjoint_kernel");
   cudaFuncAttributes attr;
   std::memset(&attr, 0, sizeof(attr));
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(m->kernel));
@@ -271,22 +276,54 @@ void gen_destroy(GenModule* m) {
   delete m;
 }
 
+namespace {
+
+// The dynamic shared-memory limit above 48 KB, set once per kernel, device
+// and size under the module's lock.
+cudaError_t ensure_smem(GenModule* m, int which, const void* fn, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(m->mutex);
+  if ((int)smem > m->configured_smem[which][dev]) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    m->configured_smem[which][dev] = (int)smem;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
 cudaError_t gen_launch(GenModule* m, const SolveParams& p, int grid, size_t smem, cudaStream_t stream) {
   const void* fn = reinterpret_cast<const void*>(m->kernel);
-  if (smem > 48 * 1024) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(m->mutex);
-    if ((int)smem > m->configured_smem[dev]) {
-      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      m->configured_smem[dev] = (int)smem;
-    }
-  }
+  cudaError_t e = ensure_smem(m, 0, fn, smem);
+  if (e != cudaSuccess) return e;
   SolveParams q = p;
   void* args[] = {&q};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(32), args, smem, stream);
+}
+
+cudaError_t gen_launch_adjoint(GenModule* m, const AdjParams& a, int grid, size_t smem, cudaStream_t stream) {
+  const void* fn = reinterpret_cast<const void*>(m->adjoint_kernel);
+  cudaError_t e = ensure_smem(m, 2, fn, smem);
+  if (e != cudaSuccess) return e;
+  AdjParams q = a;
+  void* args[] = {&q};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(32), args, smem, stream);
+}
+
+cudaError_t gen_launch_multi(GenModule* m, const SolveParams* batches, int nb, const int32_t* starts,
+                             int32_t* queue, double* scratch, int64_t slot_doubles, int grid, size_t smem,
+                             cudaStream_t stream) {
+  const void* fn = reinterpret_cast<const void*>(m->multi_kernel);
+  cudaError_t e = ensure_smem(m, 1, fn, smem);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(queue, 0, sizeof(int32_t), stream);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&batches, &nb, &starts, &queue, &scratch, &slot_doubles};
   return cudaLaunchKernel(fn, dim3(grid), dim3(32), args, smem, stream);
 }
 

@@ -17,9 +17,11 @@
 
 #ifdef FO_LINK_GENERATED
 // The mechanism's generated factorization and solves (codegen.cpp), linked in
-// per mechanism: `base` is this lane's item 0 of its scratch slot (32 lanes).
-extern "C" __device__ void fo_gen_factor(double* base, double alpha);
-extern "C" __device__ void fo_gen_solve(double* base);
+// per mechanism: `base` is this lane's item 0 of its scratch slot (32 lanes),
+// `mech` the mechanism's index in the module (several mechanisms share one).
+extern "C" __device__ void fo_gen_factor(double* base, double alpha, int mech);
+extern "C" __device__ void fo_gen_solve(double* base, int mech);
+extern "C" __device__ void fo_gen_solve_t(double* base, int mech);   // the adjoint's transposed solve
 #endif
 
 namespace fo {
@@ -604,7 +606,7 @@ __device__ void factor_any(const SolveParams& p, const Lane& ln, double alpha, c
   // the projection's algebraic-rows-only matrix takes the row loop (the same
   // factors, in the same storage, bit for bit)
   if (alg_only) factor(p, ln, alpha, negj, lu, w, alg_only);
-  else fo_gen_factor(lu - p.sl.lu * ln.L + ln.lane, alpha);
+  else fo_gen_factor(lu - p.sl.lu * ln.L + ln.lane, alpha, p.o.gen_index);
 #else
   if (p.o.variant == FO_VARIANT_PLAIN) factor(p, ln, alpha, negj, lu, w, alg_only);
   else if (p.o.variant == FO_VARIANT_COMPACT) {
@@ -633,7 +635,7 @@ __device__ void solve_into(const SolveParams& p, const Lane& ln, const double* l
   double* base = const_cast<double*>(lu) - p.sl.lu * L;
   double* xs = base + p.sl.xs * L;
   for (int i = 0; i < p.t.n; ++i) SCR(xs, i) = SCR(b, i);
-  fo_gen_solve(base + lane);
+  fo_gen_solve(base + lane, p.o.gen_index);
   for (int i = 0; i < p.t.n; ++i) SCR(x, i) = SCR(xs, i);
 #else
   if (p.o.variant == FO_VARIANT_COMPACT) {
@@ -829,8 +831,10 @@ __device__ void solve_into(const SolveParams& p, const Lane& ln, const double* l
 // damped Newton with the algebraic-rows-only matrix (alpha = 1), accepted on
 // the weighted correction, with backtracking line search. Returns true on
 // convergence; on failure Y is restored to its value on entry.
+// Every accepted update (Y += step * delta on the algebraic rows) is traced
+// as (0, step, q, 2), so that the adjoint can replay the same updates.
 __device__ __noinline__ bool project(const SolveParams& p, const Lane& ln, double* Y, double* scr, double* w, double* red,
-                        ProjectionCounts& pc) {
+                        ProjectionCounts& pc, int g, int& nrec) {
   const int L = ln.L, lane = ln.lane;
   const int n = p.t.n;
   double* G = scr + p.sl.f0 * L;
@@ -866,7 +870,7 @@ __device__ __noinline__ bool project(const SolveParams& p, const Lane& ln, doubl
       for (int i = 0; i < n; ++i) SCR(orig, i) = SCR(Y, i);
       have_orig = true;
     }
-    double step = 1.0;
+    double step = 1.0, step_used = 0.0;
     bool accepted = false;
     for (int bt = 0; bt <= max_backtracks; ++bt) {
       for (int i = 0; i < n; ++i) {
@@ -874,7 +878,7 @@ __device__ __noinline__ bool project(const SolveParams& p, const Lane& ln, doubl
         if (__ldg(p.t.mass + i) == 0.0) v = __dadd_rn(v, __dmul_rn(step, SCR(delta, i)));
         SCR(cand, i) = v;
       }
-      const double step_used = step;
+      step_used = step;
       step = __dmul_rn(step, factor_bt);
       if (!alg_finite(p, ln, cand)) continue;
       alg_residual(p, ln, cand, rr, Gc);
@@ -895,6 +899,7 @@ __device__ __noinline__ bool project(const SolveParams& p, const Lane& ln, doubl
       }
     }
     if (!accepted) break;
+    trace_record(p, g, nrec, 0.0, step_used, q, 2.0);
     for (int i = 0; i < n; ++i) SCR(Y, i) = SCR(cand, i);
   }
   if (have_orig)
@@ -936,7 +941,7 @@ __device__ __noinline__ void solve_group_restarting(const SolveParams& p, int g,
   const double nsize = (double)(C * n);
   int status = -1;
   ProjectionCounts pc;
-  if (p.t.has_constraints && !project(p, ln, Y, scr, w, red, pc)) status = FO_STATUS_PROJECTION_FAILED;
+  if (p.t.has_constraints && !project(p, ln, Y, scr, w, red, pc, g, nrec)) status = FO_STATUS_PROJECTION_FAILED;
   c_rhs += pc.rhs;
   c_jac += pc.jac;
   c_lu += pc.lu;
@@ -1202,7 +1207,7 @@ __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, 
   int status = -1;  // running
   const double nsize = (double)(C * n);
   ProjectionCounts pc;
-  if (p.t.has_constraints && !project(p, ln, Y, scr, w, red, pc)) {
+  if (p.t.has_constraints && !project(p, ln, Y, scr, w, red, pc, g, nrec)) {
     status = FO_STATUS_PROJECTION_FAILED;   // Y restored, no step taken
     proposed = h_next;                      // the carried proposal is left as it was
   }

@@ -4,7 +4,9 @@ A ``Part`` is one mechanism's cells: state (n, C) and rate constants (R, C) in
 HBM with cells fastest, per-group controller memory, counters and statuses, and
 optionally the photolysis columns that follow the diurnal factor. ``MultiBatch``
 integrates every part over an interval with one ``fo_multi_launch`` (blocks pull
-groups of all mechanisms from one device queue, largest mechanism first) after
+groups of all mechanisms from one device queue, largest mechanism first; with
+the generated kernel, one module holds every mechanism's own factorization and
+solves) after
 one photolysis update per part; the interval's time lives on the device, so the
 same captured CUDA graph replays every interval. This is the device form of the
 reference's scenario loop (fastode/ts1.py:196-222) over several mechanisms.
@@ -61,9 +63,8 @@ class Part:
 
     def desc(self) -> _abi.BatchDesc:
         o = self.alg.options()
-        if o.variant == _abi.VARIANTS["generated"]:
-            # one launch runs several mechanisms: the table-driven kernel
-            o.variant = _abi.VARIANTS["compact"]
+        if o.variant == _abi.VARIANTS["generated"] and self.max_cells > 32:
+            o.variant = _abi.VARIANTS["compact"]     # generated code runs groups of at most 32 cells
         return _abi.BatchDesc(self.plan.handle.value, o, self.ngroups, self.offsets.data_ptr(),
                               self.max_cells, self.Y.data_ptr(), 1, self.C, self.k.data_ptr(), 1, self.C,
                               self.atol.data_ptr(), self.rtol, self.dt, self.memory.data_ptr(),
@@ -72,7 +73,13 @@ class Part:
     def smem_per_block(self) -> int:
         lanes = ((self.max_cells + 31) // 32) * 32
         kernel = getattr(self.alg, "kernel", "pipelined")
+        if kernel == "generated" and self.max_cells <= 32:
+            # the reduction buffer, and the projection's work row of a constrained mechanism
+            return 8 * (32 + (self.n * lanes if self.plan.has_constraints else 0))
         return 8 * (32 + self.plan.smem_items("compact" if kernel == "generated" else kernel) * lanes)
+
+    def generated(self) -> bool:
+        return getattr(self.alg, "kernel", "") == "generated" and self.max_cells <= 32
 
     def reset(self):
         self.Y.copy_(self.Y0)
@@ -96,7 +103,10 @@ def default_slots(parts, device_index: int) -> int:
     import torch
     sms = torch.cuda.get_device_properties(device_index).multi_processor_count
     smem = max(p.smem_per_block() for p in parts)
-    per_sm = max(1, min(8, SMEM_PER_SM // smem))
+    # the generated kernel is register-bound at sixteen one-warp blocks per
+    # SM (128 registers per thread); the table-driven ones at eight
+    cap = 16 if all(p.generated() for p in parts) else 8
+    per_sm = max(1, min(cap, SMEM_PER_SM // smem))
     return sms * per_sm
 
 

@@ -167,7 +167,9 @@ typedef struct fo_options {
  * vector staged at a time, the other half in global memory, so a group needs
  * about half the shared memory and twice as many groups stay resident per SM.
  * The factors are those of PIPELINED bit for bit; the solves differ in
- * summation order (roundoff). fo_adjoint_interval runs PIPELINED. */
+ * summation order (roundoff). fo_adjoint_interval runs PIPELINED for COMPACT
+ * (its transposed solves need the whole vector on chip) and the generated
+ * adjoint for GENERATED. */
 #define FO_VARIANT_COMPACT 2
 /* GENERATED runs the mechanism's own factorization and solves, generated as
  * straight-line code from its fill pattern and compiled when the plan is
@@ -277,7 +279,11 @@ int fo_solve(const fo_plan* plan, const fo_options* opt,
  * fo_multi_workspace_bytes) and writes the batch table into it (synchronous);
  * fo_multi_launch then only resets the queue and launches, so it can be
  * captured in a CUDA graph and replayed once per interval. The pointers given
- * to prepare must stay valid for every launch.
+ * to prepare must stay valid for every launch. With FO_VARIANT_GENERATED in
+ * every batch (groups of at most 32 cells), prepare generates and links one
+ * module holding every distinct mechanism's factorization and solves (the
+ * default cache of fo_plan_generate applies) and the launch runs it; a mix of
+ * generated and table-driven batches is refused (FO_E_UNSUPPORTED).
  */
 typedef struct fo_batch_desc {
   const fo_plan* plan;
@@ -327,8 +333,15 @@ int fo_advance_clock(double* t_dev, double dt, void* stream);
  *        dL/dlog k of every cell and reaction.
  * Groups with more than max_steps steps get FO_STATUS_TOO_MANY_STEPS; a
  * non-finite adjoint FO_STATUS_NAN_OR_INF. Workspace: fo_adjoint_workspace_bytes.
- * One block per group; the projection of constrained systems is not
- * differentiated (their checkpoints are taken after it).
+ * One block per group. Constrained systems (mass 0 rows): the consistent-
+ * initialization projection that starts every call (fastode/solvers.py:100-178)
+ * is part of the map and is differentiated too. proj_steps[proj_ptr[g] ..
+ * proj_ptr[g+1]) are the line-search steps of the Newton updates the forward
+ * call applied to group g, in order (its trace's records of outcome 2); the
+ * updates are replayed with those steps held fixed and their reverse sweep is
+ * a transposed solve with the projection's matrix, the forcing's
+ * vector-Jacobian product and the Jacobian's second derivatives. NULL, NULL:
+ * no updates (required for unconstrained mechanisms).
  */
 int fo_adjoint_workspace_bytes(const fo_plan* plan, int32_t ngroups, int32_t max_group_cells, int32_t max_steps,
                                size_t* bytes);
@@ -337,7 +350,8 @@ int fo_adjoint_interval(const fo_plan* plan, const fo_options* opt, int32_t ngro
                         const double* Y, int64_t y_cell_stride, int64_t y_species_stride,
                         const double* k, int64_t k_cell_stride, int64_t k_reaction_stride,
                         const double* atol, double dt,
-                        const int32_t* step_ptr, const double* steps, int32_t max_steps, int32_t mode,
+                        const int32_t* step_ptr, const double* steps, int32_t max_steps,
+                        const int32_t* proj_ptr, const double* proj_steps, int32_t mode,
                         double* lam, int64_t lam_cell_stride, int64_t lam_species_stride,
                         double* thbar, int64_t thbar_cell_stride, int64_t thbar_reaction_stride,
                         double* Yout, int64_t yout_cell_stride, int64_t yout_species_stride,

@@ -610,15 +610,34 @@ def replay_interval(system, tab, Y, steps):
     return np.where(keep, Y, 0.0)
 
 
-def tangent_linear(mech, Y0, dY0, k_list, dlogk, steps_list, tab=None, mass=None, eps=1e-30):
+def replay_projection(system, Y, steps):
+    """The projection's accepted Newton updates of one call with their
+    line-search steps held fixed (solvers.py:110-160 without the decisions):
+    Y_alg += step * (M - J)_alg^-1 G(Y), G the forcing on the algebraic rows."""
+    alg = system.mass == 0.0
+    for step in steps:
+        G = system.rhs(Y)
+        G[:, ~alg] = 0.0
+        LU = system.factor(1.0, system.jac(Y), algebraic_rows_only=True)
+        delta = LU.solve(G)
+        Y = Y.copy()
+        Y[:, alg] += step * delta[:, alg]
+    return Y
+
+
+def tangent_linear(mech, Y0, dY0, k_list, dlogk, steps_list, tab=None, mass=None, eps=1e-30, proj_list=None):
     """Directional derivative of the fixed-step map over all intervals in
     direction (dY0, dlogk) by the complex step: exact to roundoff, because the
     map is analytic in its inputs away from the clamp's kink. k_list[i] is
-    (C, R); steps_list[i] is the list of step sizes of interval i."""
+    (C, R); steps_list[i] is the list of step sizes of interval i; with
+    constraints, proj_list[i] the line-search steps of the projection updates
+    that start interval i."""
     tab = tab or OROS3
     Y = Y0.astype(np.complex128) + 1j * eps * dY0
     scale = np.exp(1j * eps * np.asarray(dlogk))[None, :]
-    for k, steps in zip(k_list, steps_list):
+    for i, (k, steps) in enumerate(zip(k_list, steps_list)):
         system = OChem(mech, k.astype(np.complex128) * scale, mass=mass, dense=True)
+        if proj_list is not None:
+            Y = replay_projection(system, Y, proj_list[i])
         Y = replay_interval(system, tab, Y, steps)
     return np.imag(Y) / eps, np.real(Y)

@@ -112,45 +112,43 @@ def test_autograd_function(cuda):
     assert float(theta.grad.abs().sum()) > 0.0
 
 
+def host_proj_steps(traj, g, i):
+    p = traj.proj_ptr[i].cpu().numpy()
+    s = traj.proj_steps[i].cpu().numpy()
+    return s[p[g]:p[g + 1]].tolist()
+
+
 def test_constrained_rodas3_adjoint(cuda):
     """RODAS3 with ten algebraic species (mass 0, quasi-steady state): the
-    constrained synthetic workload's 32 cells. Gradients with respect to the
-    log rate constants and the state, against the oracle's tangent-linear
-    (complex step through the fixed-step RODAS3 map with the mass matrix) and
-    central differences of the device's fixed-step replay.
-
-    The projection that starts every call (fastode/solvers.py:100-178, 322-325)
-    is not differentiated. The first interval projects the inconsistent
-    initial state, so the recording starts after it; on the recorded intervals
-    no projection takes a Newton update (no line-search trial), so each one
-    leaves the state exactly as it is, the forward map is the fixed-step map
-    bit for bit, and its gradient is the fixed-step map's: leaving the
-    projection out changes the gradient by nothing."""
+    constrained synthetic workload's 32 cells over its four 60 s intervals.
+    Every call starts with the projection onto the constraints
+    (fastode/solvers.py:100-178), which here applies Newton updates in every
+    interval; the adjoint differentiates those updates (with the forward
+    run's line-search steps held fixed) as well as the RODAS3 steps.
+    Gradients with respect to the log rate constants and the state against
+    the oracle's tangent-linear (complex step through the same fixed
+    projection updates and steps, mass matrix included) and against central
+    differences of the device's replay, which reproduces the forward run."""
     from fastode_gb300 import Algorithm, RODAS3
     from fastode_gb300.adjoint import adjoint, forward_record, replay
-    from fastode_gb300.batch import Batch
     from oracle import rosenbrock as O
     torch = cuda
     f = load("rodas3_dae_160x340")
     mech = mechanism_of(f)
     mass = f["mass"]
     dt, rtol = float(f["dt"]), float(f["rtol"])
-    ks = [torch.from_numpy(np.ascontiguousarray(f["k"][i].T)).cuda() for i in range(int(f["intervals"]))]
-    alg = Algorithm(RODAS3)
-    b = Batch(mech, f["Y0"], group_size=32, algorithm=alg, mass=mass)
-    b.step(ks[0], dt, torch.from_numpy(f["atol"]).cuda(), rtol)
-    Y1 = b.state()
-    intervals = len(ks) - 1
-    traj = forward_record(mech, Y1, lambda i: ks[i + 1], dt, f["atol"], rtol, intervals, algorithm=alg, mass=mass)
-    counts = traj.batch.counts.cpu().numpy()
-    assert counts[:, 11].sum() == 0, counts          # no line-search trial: no projection moved the state
+    intervals = int(f["intervals"])
+    ks = [torch.from_numpy(np.ascontiguousarray(f["k"][i].T)).cuda() for i in range(intervals)]
+    Y0 = f["Y0"]
+    traj = forward_record(mech, Y0, lambda i: ks[i], dt, f["atol"], rtol, intervals, algorithm=Algorithm(RODAS3),
+                          mass=mass)
     assert all(s == ["converged"] for s in traj.statuses)
+    proj = [host_proj_steps(traj, 0, i) for i in range(intervals)]
+    assert sum(len(p) for p in proj) > 0, proj                     # the projection does move the state
     np.testing.assert_array_equal(replay(traj).cpu().numpy(), traj.batch.Y.cpu().numpy())
 
-    C = traj.batch.C
     rng = np.random.default_rng(5)
-    dY0 = Y1 * rng.standard_normal(Y1.shape)
-    dY0[:, mass == 0.0] = 0.0                        # perturb the differential species only
+    dY0 = Y0 * rng.standard_normal(Y0.shape)
     dth = rng.standard_normal(mech.R)
     Yend = traj.batch.state()
     lam_end = rng.standard_normal(Yend.shape) / np.maximum(np.abs(Yend), 1e-14)
@@ -158,8 +156,8 @@ def test_constrained_rodas3_adjoint(cuda):
     g_y, g_th = lam0.cpu().numpy().T, thbar.cpu().numpy().sum(axis=1)
     adj = np.sum(g_y * dY0) + np.sum(g_th * dth)
     steps = [host_steps(traj, 0, i) for i in range(intervals)]
-    tl, _ = O.tangent_linear(mech, Y1, dY0, [f["k"][i + 1] for i in range(intervals)], dth, steps,
-                             tab=O.ORODAS3, mass=mass)
+    tl, Yo = O.tangent_linear(mech, Y0, dY0, [f["k"][i] for i in range(intervals)], dth, steps,
+                              tab=O.ORODAS3, mass=mass, proj_list=proj)
     ref = np.sum(lam_end * tl)
     assert abs(adj - ref) <= 1e-8 * np.sum(np.abs(lam_end * tl)), (adj, ref)
 

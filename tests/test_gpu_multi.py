@@ -12,28 +12,34 @@ def small_parts():
     return syn.batched_uneven(n_cells=32 * 6, intervals=4, sizes=((20, 40), (60, 40), (30, 70)))
 
 
-def make_parts(wls, cuda):
+def make_parts(wls, cuda, kernel="generated"):
+    from fastode_gb300 import Algorithm
     from fastode_gb300.multi import Part
     parts = []
     for wl in wls:
         photo = np.nonzero(wl.sm.photolytic)[0]
         parts.append(Part(wl.sm.mech, wl.cells.Y0, wl.k_at(0), wl.atol, wl.rtol, wl.dt, group_size=32,
-                          photolysis=(photo, wl.sm.J[photo], wl.cells.phase)))
+                          algorithm=Algorithm(kernel=kernel), photolysis=(photo, wl.sm.J[photo], wl.cells.phase)))
     return parts
 
 
+@pytest.mark.parametrize("kernel", ["generated", "compact"])
 @pytest.mark.parametrize("graph", [True, False])
-def test_multi_launch_matches_separate_batches(cuda, graph):
+def test_multi_launch_matches_separate_batches(cuda, graph, kernel):
+    """One persistent launch over three mechanisms (with the generated kernel,
+    one module holding the three mechanisms' code) against one launch per
+    mechanism."""
+    from fastode_gb300 import Algorithm
     from fastode_gb300.batch import Batch
     from fastode_gb300.multi import MultiBatch
     torch = cuda
     wls = small_parts()
-    mb = MultiBatch(make_parts(wls, cuda))
+    mb = MultiBatch(make_parts(wls, cuda, kernel))
     intervals = 4
     mb.run(intervals, graph=graph)
     torch.cuda.synchronize()
     for wl, part in zip(wls, mb.parts):
-        b = Batch(wl.sm.mech, wl.cells.Y0, group_size=32)
+        b = Batch(wl.sm.mech, wl.cells.Y0, group_size=32, algorithm=Algorithm(kernel=kernel))
         atol = torch.from_numpy(wl.atol).cuda()
         for i in range(intervals):
             # the device clock and the photolysis kernel against host-made k:
