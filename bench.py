@@ -453,30 +453,44 @@ def run_batched(args):
     sp = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
     wls = syn.batched_uneven(n_cells=args.cells, intervals=args.steps)
     from fastode_gb300 import Algorithm
-    group_size, kernel, tuning = 32, args.kernel, None
+    chosen = [(32, args.kernel, 6) for _ in wls]
+    tuning = None
     if args.autotune:
-        # the group size and kernel of the launch, measured on 4,096 cells of
-        # the largest mechanism (one untimed and two timed intervals each)
+        # per mechanism: group size, kernel and the generated code's register
+        # tile, measured on 4,096 of its cells (one untimed and two timed
+        # intervals each)
         from fastode_gb300.tune import autotune, candidates, measure_on_device
-        big = wls[-1].subset(slice(0, 4096))
-        measure = measure_on_device(big.sm.mech, big.cells.Y0, big.k_at, big.dt, big.atol, big.rtol)
         from fastode_gb300.plan import plan_for
-        bp = plan_for(big.sm.mech)
-        smem = {k: bp.smem_items(k) for k in ("pipelined", "plain", "compact")}
-        res = autotune(measure, smem, candidates(smem, group_sizes=(16, 32, 64),
-                                                 kernels=("compact", "pipelined", "plain"), persistent=(True,)))
-        group_size, kernel = res.best.group_size, res.best.kernel
-        tuning = {"sample": "4,096 cells of ros3-210x500, intervals 1-2 timed",
-                  "table": [{"kernel": c.kernel, "group_size": c.group_size,
-                             "cell_intervals_per_s": v} for c, v in res.table],
-                  "chosen": {"kernel": kernel, "group_size": group_size}}
+        tiles = tuple(int(t) for t in str(getattr(args, "tune_tiles", "6")).split(","))
+        tuning = []
+        for j, wl in enumerate(wls):
+            sample = wl.subset(slice(0, min(4096, wl.cells.C)))
+            measure = measure_on_device(sample.sm.mech, sample.cells.Y0, sample.k_at, sample.dt, sample.atol,
+                                        sample.rtol)
+            bp = plan_for(sample.sm.mech)
+            smem = {k: bp.smem_items(k) for k in ("pipelined", "plain", "compact")}
+            smem["generated"] = 0
+            res = autotune(measure, smem, candidates(smem, group_sizes=(16, 32), kernels=("generated", "compact"),
+                                                     persistent=(True,), tiles=tiles))
+            if res.best.kernel != "generated":       # one launch runs one family of kernels
+                gen = [(c, v) for c, v in res.table if c.kernel == "generated" and v is not None]
+                best = max(gen, key=lambda cv: cv[1])[0] if gen else res.best
+            else:
+                best = res.best
+            chosen[j] = (best.group_size, best.kernel, best.tile)
+            tuning.append({"mechanism": wl.name, "sample": f"{sample.cells.C} cells, intervals 1-2 timed",
+                           "table": [{"kernel": c.kernel, "group_size": c.group_size, "tile": c.tile,
+                                      "cell_intervals_per_s": v} for c, v in res.table],
+                           "chosen": {"kernel": best.kernel, "group_size": best.group_size, "tile": best.tile}})
     parts = []
-    for wl in wls:
+    for wl, (group_size, kernel, tile) in zip(wls, chosen):
         k, photo = _device_rates(lib, wl.sm, wl.cells, dev, sp)
         p = Part(wl.sm.mech, torch.from_numpy(wl.cells.Y0).to(dev), k.t(), wl.atol, wl.rtol, wl.dt,
-                 group_size=group_size, algorithm=Algorithm(kernel=kernel, ordering=args.ordering),
+                 group_size=group_size, algorithm=Algorithm(kernel=kernel, ordering=args.ordering, tile=tile),
                  photolysis=(photo, wl.sm.J[photo], wl.cells.phase))
         parts.append(p)
+    kernel = chosen[0][1]
+    group_size = sorted({c[0] for c in chosen})
     fma_rate = C.c_double()
     _abi.check(lib.fo_fp64_fma_rate(C.byref(fma_rate)), "fo_fp64_fma_rate")
     mb = MultiBatch(parts)
@@ -768,7 +782,11 @@ def main():
                          "three-mechanism persistent launch; adjoint: forward+adjoint cost; dae: the RODAS3 "
                          "constrained workload with its adjoint cost")
     ap.add_argument("--autotune", action="store_true",
-                    help="batched workload: choose group size and kernel with the autotuner on a sample")
+                    help="batched workload: choose group size, kernel and register tile per mechanism with the "
+                         "autotuner on a sample")
+    ap.add_argument("--tune-tiles", default="6",
+                    help="batched workload with --autotune: register tiles of the generated code to try, e.g. "
+                         "4,6,8 (each one compiles the mechanism once)")
     ap.add_argument("--fd-directions", type=int, default=2,
                     help="central-difference directions checking the adjoint gradient")
     ap.add_argument("--adjoint-intervals", type=int, default=0,

@@ -99,6 +99,7 @@ SIGNATURES = {
     "fo_plan_permutation": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "fo_workspace_bytes": (C.c_int, [_P, _I32, _I32, C.POINTER(C.c_size_t)]),
     "fo_plan_generate": (C.c_int, [_P, C.c_char_p, C.POINTER(GenInfo)]),
+    "fo_plan_set_generation": (C.c_int, [_P, _I32, _I32]),
     "fo_generate_check": (C.c_int, [C.POINTER(MechanismDesc), _I32, _I32, C.POINTER(GenInfo)]),
     "fo_solve": (C.c_int, [_P, C.POINTER(Options), _I32, _P, _I32,
                            _P, _I64, _I64, _P, _I64, _I64, _P, _D, _D,

@@ -32,7 +32,7 @@ class Batch:
         import torch
         self.torch = torch
         self.alg = algorithm if algorithm is not None else Algorithm()
-        self.plan = plan_for(mech, mass, self.alg.ordering)
+        self.plan = plan_for(mech, mass, self.alg.ordering, getattr(self.alg, "tile", 6))
         dev = torch.device("cuda", self.plan.device)
         self.dev = dev
         Y0 = Y0 if isinstance(Y0, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(Y0, dtype=np.float64))
@@ -99,7 +99,7 @@ class HostState:
     def __init__(self, mech, C_cells, n, R, group_size, algorithm, mass, slots, dev):
         import torch
         self.alg = algorithm if algorithm is not None else Algorithm()
-        self.plan = plan_for(mech, mass, self.alg.ordering)
+        self.plan = plan_for(mech, mass, self.alg.ordering, getattr(self.alg, "tile", 6))
         offs = group_offsets(C_cells, group_size)
         self.ngroups = len(offs) - 1
         self.max_cells = int(np.max(np.diff(offs)))

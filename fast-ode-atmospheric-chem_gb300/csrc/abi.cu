@@ -34,6 +34,7 @@ struct fo_plan {
   void* blob = nullptr;  // device copy of every table
   int device = -1;
   fo::GenModule* gen = nullptr;  // the generated variant's module (fo_plan_generate)
+  fo::GenOptions gen_options;    // its register tile and solve block (fo_plan_set_generation)
   fo_gen_info gen_info{};
   std::mutex gen_mutex;
 };
@@ -171,7 +172,7 @@ int fo_generate_check(const fo_mechanism_desc* mech, int32_t ordering, int32_t l
     fo::HostTables t;
     std::string err = fo::build_tables(*mech, ordering, &t);
     if (!err.empty()) return fail(FO_E_INVALID, err);
-    int rc = fo::gen_check(t, link != 0, info, &err);
+    int rc = fo::gen_check(t, fo::GenOptions(), link != 0, info, &err);
     if (rc != FO_OK) return fail(rc, err);
   } catch (const std::bad_alloc&) {
     return fail(FO_E_ALLOC, "host allocation failed");
@@ -299,13 +300,25 @@ int fo_plan_permutation(const fo_plan* plan, int32_t* perm) {
   return FO_OK;
 }
 
+int fo_plan_set_generation(fo_plan* plan, int32_t tile, int32_t solve_block) {
+  if (!plan) return fail(FO_E_INVALID, "null plan");
+  if (tile < 1 || tile > 16 || solve_block < 1 || solve_block > 64)
+    return fail(FO_E_INVALID, "tile must be 1..16 and solve_block 1..64");
+  std::lock_guard<std::mutex> lock(plan->gen_mutex);
+  if (plan->gen && (plan->gen_options.tile != tile || plan->gen_options.solve_block != solve_block))
+    return fail(FO_E_INVALID, "the plan's generated module was made with other options");
+  plan->gen_options.tile = tile;
+  plan->gen_options.solve_block = solve_block;
+  return FO_OK;
+}
+
 int fo_plan_generate(fo_plan* plan, const char* cache_dir, fo_gen_info* info) {
   if (!plan) return fail(FO_E_INVALID, "null plan");
   std::lock_guard<std::mutex> lock(plan->gen_mutex);
   if (!plan->gen) {
     std::string err;
     fo_gen_info gi;
-    int rc = fo::gen_create({&plan->host}, cache_dir, &plan->gen, &gi, &err);
+    int rc = fo::gen_create({&plan->host}, {plan->gen_options}, cache_dir, &plan->gen, &gi, &err);
     if (rc != FO_OK) return fail(rc, err);
     plan->gen_info = gi;
   }
@@ -536,13 +549,17 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
   if (ngen != 0 && ngen != nb)
     return fail(FO_E_UNSUPPORTED, "one launch runs either the generated variant for every batch or for none");
   std::vector<const fo::HostTables*> tables;
+  std::vector<fo::GenOptions> gen_opts;
   if (ngen) {
     if (L.lanes != 32) return fail(FO_E_UNSUPPORTED, "FO_VARIANT_GENERATED runs groups of at most 32 cells");
     for (int j = 0; j < nb; ++j) {
-      const fo::HostTables* t = &b[order[j]].plan->host;
-      auto it = std::find(tables.begin(), tables.end(), t);
+      const fo_plan* pl = b[order[j]].plan;
+      auto it = std::find(tables.begin(), tables.end(), &pl->host);
       params[j].o.gen_index = (int)(it - tables.begin());
-      if (it == tables.end()) tables.push_back(t);
+      if (it == tables.end()) {
+        tables.push_back(&pl->host);
+        gen_opts.push_back(pl->gen_options);
+      }
     }
   }
   int dev = 0, smem_max = 0;
@@ -556,7 +573,7 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
   if (!m) return fail(FO_E_ALLOC, "host allocation failed");
   if (ngen) {
     std::string err;
-    rc = fo::gen_create(tables, nullptr, &m->gen, nullptr, &err);
+    rc = fo::gen_create(tables, gen_opts, nullptr, &m->gen, nullptr, &err);
     if (rc != FO_OK) {
       delete m;
       return fail(rc, err);

@@ -372,14 +372,18 @@ std::string function(const char* name, const char* params, const Ptx& x, const s
 
 }  // namespace
 
-std::string generate_ptx(const std::vector<const HostTables*>& ts, const GenOptions& o, int64_t* fma_count) {
-  if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64)
-    throw std::invalid_argument("tile sizes out of range");
-  if (ts.empty()) throw std::invalid_argument("no mechanism");
+std::string generate_ptx(const std::vector<const HostTables*>& ts, const std::vector<GenOptions>& os,
+                         int64_t* fma_count) {
+  if (ts.empty() || os.size() != ts.size()) throw std::invalid_argument("one set of options per mechanism");
+  for (const GenOptions& o : os)
+    if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64)
+      throw std::invalid_argument("tile sizes out of range");
   Ptx f, s, st;
   std::vector<std::string> fb, sb, tb;
   int64_t total = 0;
-  for (const HostTables* t : ts) {
+  for (size_t m = 0; m < ts.size(); ++m) {
+    const HostTables* t = ts[m];
+    const GenOptions& o = os[m];
     const ScratchLayout sl = layout_of(*t);
     const Pattern P = pattern_of(*t);
     int64_t nfma = 0;
@@ -414,7 +418,7 @@ std::string generate_ptx(const std::vector<const HostTables*>& ts, const GenOpti
 }
 
 std::string generate_ptx(const HostTables& t, const GenOptions& o, int64_t* fma_count) {
-  return generate_ptx(std::vector<const HostTables*>{&t}, o, fma_count);
+  return generate_ptx(std::vector<const HostTables*>{&t}, std::vector<GenOptions>{o}, fma_count);
 }
 
 }  // namespace fo

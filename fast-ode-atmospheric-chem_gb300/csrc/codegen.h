@@ -42,7 +42,7 @@ std::string generate_ptx(const HostTables& t, const GenOptions& o, int64_t* fma_
 
 // The same for several mechanisms in one module: `mech` is the mechanism's
 // index in `ts` and selects its code.
-std::string generate_ptx(const std::vector<const HostTables*>& ts, const GenOptions& o,
+std::string generate_ptx(const std::vector<const HostTables*>& ts, const std::vector<GenOptions>& os,
                          int64_t* fma_count = nullptr);
 
 }  // namespace fo

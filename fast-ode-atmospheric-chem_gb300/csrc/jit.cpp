@@ -189,14 +189,13 @@ struct GenModule {
   int configured_smem[3][64] = {};
 };
 
-int gen_create(const std::vector<const HostTables*>& ts, const char* cache_dir, GenModule** out, fo_gen_info* info,
-               std::string* err) {
+int gen_create(const std::vector<const HostTables*>& ts, const std::vector<GenOptions>& opts, const char* cache_dir,
+               GenModule** out, fo_gen_info* info, std::string* err) {
   const auto t0 = std::chrono::steady_clock::now();
   *out = nullptr;
-  GenOptions opt;
   std::string ptx;
   try {
-    ptx = generate_ptx(ts, opt);
+    ptx = generate_ptx(ts, opts);
   } catch (const std::exception& e) {
     *err = std::string("code generation failed: ") + e.what();
     return FO_E_INVALID;
@@ -238,7 +237,7 @@ int gen_create(const std::vector<const HostTables*>& ts, const char* cache_dir, 
     std::memset(info, 0, sizeof(*info));
     info->from_cache = cached ? 1 : 0;
     info->registers = attr.numRegs;
-    info->tile = opt.tile;
+    info->tile = opts.empty() ? 0 : opts[0].tile;
     info->local_bytes = (int32_t)attr.localSizeBytes;
     info->ptx_bytes = (int64_t)ptx.size();
     info->cubin_bytes = (int64_t)cubin.size();
@@ -248,9 +247,8 @@ int gen_create(const std::vector<const HostTables*>& ts, const char* cache_dir, 
   return FO_OK;
 }
 
-int gen_check(const HostTables& t, bool do_link, fo_gen_info* info, std::string* err) {
+int gen_check(const HostTables& t, const GenOptions& opt, bool do_link, fo_gen_info* info, std::string* err) {
   const auto t0 = std::chrono::steady_clock::now();
-  GenOptions opt;
   std::string ptx;
   try {
     ptx = generate_ptx(t, opt);

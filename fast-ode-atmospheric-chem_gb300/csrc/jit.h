@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "codegen.h"
 #include "device.cuh"
 #include "fastode_gb300.h"
 #include "symbolic.h"
@@ -17,11 +18,11 @@ struct GenModule;
 // Generate, link (or take from the cache in cache_dir; null: the default
 // cache, empty: none) and load the module of one or several plans' tables
 // (mechanism index = position in ts).
-int gen_create(const std::vector<const HostTables*>& ts, const char* cache_dir, GenModule** out, fo_gen_info* info,
-               std::string* err);
+int gen_create(const std::vector<const HostTables*>& ts, const std::vector<GenOptions>& opts, const char* cache_dir,
+               GenModule** out, fo_gen_info* info, std::string* err);
 void gen_destroy(GenModule* m);
 // Generate (and, with do_link, link) without a device: no module is loaded.
-int gen_check(const HostTables& t, bool do_link, fo_gen_info* info, std::string* err);
+int gen_check(const HostTables& t, const GenOptions& opt, bool do_link, fo_gen_info* info, std::string* err);
 // One launch of the generated integrator kernel: grid blocks of 32 lanes.
 cudaError_t gen_launch(GenModule* m, const SolveParams& p, int grid, size_t smem, cudaStream_t stream);
 // One launch of the generated adjoint kernel (fo_adjoint_interval): grid

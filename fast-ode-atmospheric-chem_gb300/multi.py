@@ -35,7 +35,7 @@ class Part:
         for the reactions whose k follows J * max(0, cos(phase + omega t))."""
         import torch
         self.alg = algorithm if algorithm is not None else Algorithm()
-        self.plan = plan_for(mech, mass, self.alg.ordering)
+        self.plan = plan_for(mech, mass, self.alg.ordering, getattr(self.alg, "tile", 6))
         dev = device if device is not None else torch.device("cuda", self.plan.device)
         Y0 = torch.as_tensor(np.asarray(Y0, dtype=np.float64)) if not isinstance(Y0, torch.Tensor) else Y0
         k = torch.as_tensor(np.asarray(k, dtype=np.float64)) if not isinstance(k, torch.Tensor) else k

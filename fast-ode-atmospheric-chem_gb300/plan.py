@@ -56,7 +56,7 @@ def analyze(mech, ordering: str = "auto", mass=None) -> dict:
 class Plan:
     """A device plan for one mechanism and mass vector."""
 
-    def __init__(self, mech, mass=None, ordering: str = "auto"):
+    def __init__(self, mech, mass=None, ordering: str = "auto", tile: int = 6):
         import torch
         if not torch.cuda.is_available():
             raise RuntimeError("fastode_gb300 needs a CUDA GPU: there is no host integrator")
@@ -73,6 +73,8 @@ class Plan:
                                              C.byref(handle)), "fo_plan_create")
         self.handle = handle
         self._finalizer = weakref.finalize(self, _abi.lib().fo_plan_destroy, handle)
+        self.tile = int(tile)
+        _abi.check(_abi.lib().fo_plan_set_generation(handle, self.tile, 8), "fo_plan_set_generation")
         info = _abi.PlanInfo()
         _abi.check(_abi.lib().fo_plan_info_get(handle, C.byref(info)), "fo_plan_info_get")
         self.info = info.as_dict()
@@ -146,15 +148,15 @@ class Plan:
 _cache: dict = {}
 
 
-def plan_for(mech, mass=None, ordering: str = "auto") -> Plan:
-    """The cached plan of a mechanism object (reference or this package's)
-    and mass vector on the current device."""
+def plan_for(mech, mass=None, ordering: str = "auto", tile: int = 6) -> Plan:
+    """The cached plan of a mechanism object (reference or this package's),
+    mass vector and generated-code tile on the current device."""
     import torch
     m = np.ones(mech.n) if mass is None else np.asarray(mass, dtype=np.float64)
-    key = (id(mech), m.tobytes(), ordering, torch.cuda.current_device())
+    key = (id(mech), m.tobytes(), ordering, int(tile), torch.cuda.current_device())
     hit = _cache.get(key)
     if hit is not None and hit.mech is mech:
         return hit
-    p = Plan(mech, m, ordering)
+    p = Plan(mech, m, ordering, tile)
     _cache[key] = p
     return p

@@ -88,7 +88,7 @@ def _device_solve(solver, system, Y, dt, atol, rtol, counts: Counts, mem):
     C_cells, n = Y.shape
     if n != system.n:
         raise ValueError(f"Y has {n} species, the system {system.n}")
-    plan = plan_for(system.mech, system.mass, solver.ordering)
+    plan = plan_for(system.mech, system.mass, solver.ordering, getattr(solver, "tile", 6))
     k = _k_rows(system, C_cells)
     atol = np.array(np.broadcast_to(np.asarray(atol, dtype=np.float64), (n,)))
     dev = torch.device("cuda", plan.device)
@@ -125,7 +125,7 @@ class Algorithm:
     def __init__(self, tableau: Tableau = ROS3, controller: str = "h211b", b: float = 4.0,
                  safety: float = 0.9, fac_min: float = 0.2, fac_max: float = 6.0,
                  carry: bool = True, quantize: bool = True, max_steps: int = 1000,
-                 carry_memory: bool = True, ordering: str = "auto", kernel: str = "generated"):
+                 carry_memory: bool = True, ordering: str = "auto", kernel: str = "generated", tile: int = 6):
         """The reference's arguments, plus two of the device path: the
         fill-reducing ``ordering`` of the sparse LU and the ``kernel`` variant:
         "generated", the mechanism's own factorization and solves generated as
@@ -135,7 +135,8 @@ class Algorithm:
         vector in shared memory; "pipelined", whole rows in shared memory; or
         "plain", the direct loops. All give the same factors; "generated" and
         "plain" give the same solutions bit for bit, the others differ in the
-        solves' summation order."""
+        solves' summation order. ``tile``: the generated factorization's
+        register tiles (rows and columns), a speed choice only."""
         self.tableau = tableau
         self.controller = controller
         self.b = b
@@ -150,6 +151,7 @@ class Algorithm:
         if kernel not in _abi.VARIANTS:
             raise ValueError(f"kernel must be one of {sorted(_abi.VARIANTS)}")
         self.kernel = kernel
+        self.tile = int(tile)
         tableau_id(tableau)
 
     def new_memory(self) -> Memory:
@@ -189,8 +191,9 @@ class RestartingLoop(Algorithm):
     name = "restarting"
 
     def __init__(self, tableau: Tableau = ROS3, max_steps: int = 1000, step_change_rows: bool = True,
-                 ordering: str = "auto", kernel: str = "generated"):
-        super().__init__(tableau, controller="elementary", max_steps=max_steps, ordering=ordering, kernel=kernel)
+                 ordering: str = "auto", kernel: str = "generated", tile: int = 6):
+        super().__init__(tableau, controller="elementary", max_steps=max_steps, ordering=ordering, kernel=kernel,
+                         tile=tile)
         self.step_change_rows = step_change_rows
 
     def new_memory(self):
@@ -223,7 +226,7 @@ class BackwardEuler:
 
     def __init__(self, max_iterations: int = 11, reductions=(0.5, 0.5, 0.5, 0.5, 0.1),
                  small: float = 1.0e-40, max_steps: int = 1_000_000, ordering: str = "auto",
-                 kernel: str = "generated"):
+                 kernel: str = "generated", tile: int = 6):
         self.max_iterations = max_iterations
         self.reductions = tuple(float(r) for r in reductions)
         if len(self.reductions) > 8:
@@ -236,6 +239,7 @@ class BackwardEuler:
         if kernel not in _abi.VARIANTS:
             raise ValueError(f"kernel must be one of {sorted(_abi.VARIANTS)}")
         self.kernel = kernel
+        self.tile = int(tile)
 
     def new_memory(self):
         return None

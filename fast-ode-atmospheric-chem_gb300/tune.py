@@ -1,5 +1,21 @@
-"""Autotuner: choose the kernel variant, the group size and the launch shape
-per mechanism by measuring them on a sample of the workload.
+"""Autotuner: choose the kernel variant, the group size, the launch shape and
+the generated code's register tiling per mechanism by measuring them on a
+sample of the workload.
+
+The dimensions:
+  * kernel: the generated variant (the mechanism's own straight-line code) or
+    a table-driven one (compact, pipelined, plain);
+  * group size: cells per group (one thread per cell; the generated variant
+    runs groups of up to 32 cells);
+  * tile: the rows and columns of the generated factorization's register
+    tiles (register tiling of the factorization: the larger the tile, the
+    fewer loads per multiply-add and the more registers), measured against
+    the occupancy it costs;
+  * persistent: one block per group, or persistent blocks pulling a queue.
+Threads per cell is one: on GB300 a double-precision warp instruction costs
+the same issue slot whether one lane or 32 are active, and a second lane per
+cell would wait on the first through every pivot of the elimination, so every
+lane integrates a cell of its own.
 
 Group size is a numerical choice as well as a speed one: the cells of a group
 share one step sequence and one error norm (the reference's groups of 32,
@@ -23,6 +39,7 @@ class Config:
     kernel: str = "compact"       # FO_VARIANT_*
     group_size: int = 32
     persistent: bool = False      # one block per group, or persistent blocks pulling a queue
+    tile: int = 6                 # the generated factorization's register tile
 
 
 @dataclass
@@ -40,17 +57,20 @@ def _items(smem_doubles_per_cell, kernel: str) -> int:
 
 
 def fits(smem_doubles_per_cell, group_size: int, kernel: str = "pipelined") -> bool:
+    if kernel == "generated" and group_size > 32:
+        return False                      # the generated code runs groups of at most 32 cells
     lanes = ((group_size + 31) // 32) * 32
     return 8 * (32 + _items(smem_doubles_per_cell, kernel) * lanes) <= SMEM_LIMIT
 
 
 def candidates(smem_doubles_per_cell: int, group_sizes=(16, 32, 64, 128),
-               kernels=("compact", "pipelined", "plain"), persistent=(False, True)) -> list:
+               kernels=("compact", "pipelined", "plain"), persistent=(False, True), tiles=(6,)) -> list:
     out = []
     for k in kernels:
         for g in group_sizes:
             for p in persistent:
-                out.append(Config(k, g, p))
+                for t in (tiles if k == "generated" else (6,)):
+                    out.append(Config(k, g, p, t))
     return out
 
 
@@ -88,11 +108,14 @@ def measure_on_device(mech, Y0, k_of, dt, atol, rtol, warm: int = 1, timed: int 
     at = torch.from_numpy(np.ascontiguousarray(atol, dtype=np.float64)).cuda()
 
     def measure(c: Config) -> float:
-        alg = Algorithm(kernel=c.kernel)
+        alg = Algorithm(kernel=c.kernel, tile=c.tile)
         b = Batch(mech, Y0, group_size=c.group_size, algorithm=alg, mass=mass)
         if c.persistent:
             lanes = ((c.group_size + 31) // 32) * 32
-            per_sm = max(1, min(8, SMEM_LIMIT // (8 * (32 + b.plan.smem_items(c.kernel) * lanes))))
+            if c.kernel == "generated":
+                per_sm = 16                   # register-bound: 128 registers per thread
+            else:
+                per_sm = max(1, min(8, SMEM_LIMIT // (8 * (32 + b.plan.smem_items(c.kernel) * lanes))))
             b = Batch(mech, Y0, group_size=c.group_size, algorithm=alg, mass=mass,
                       slots=torch.cuda.get_device_properties(b.plan.device).multi_processor_count * per_sm)
         for i in range(warm):

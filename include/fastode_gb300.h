@@ -220,10 +220,18 @@ int fo_plan_permutation(const fo_plan* plan, int32_t* perm);
  * nvJitLink is missing or linking fails (fo_last_error has the log). */
 int fo_plan_generate(fo_plan* plan, const char* cache_dir, fo_gen_info* info);
 
+/* The generated code's shape for this plan, before fo_plan_generate (and
+ * before the plan joins a generated several-mechanism launch): the rows and
+ * columns of the factorization's register tiles (1..16, default 6) and the
+ * rows of a block of the solves (1..64, default 8). A tuning choice that
+ * changes no result: every tile gives the same factors bit for bit. Refused
+ * once the plan's module exists with other options. */
+int fo_plan_set_generation(fo_plan* plan, int32_t tile, int32_t solve_block);
+
 /* Host-only check of the generated variant (no device needed): generate the
  * mechanism's code for the given ordering and, when link is nonzero, link it
- * with the integrator (nvJitLink); info gets the sizes and the time taken.
- * No counterpart in the reference. */
+ * with the integrator (nvJitLink); info gets the sizes and the time taken
+ * (default tile and solve block). No counterpart in the reference. */
 int fo_generate_check(const fo_mechanism_desc* mech, int32_t ordering, int32_t link, fo_gen_info* info);
 
 /* Bytes of device workspace fo_solve needs for `slots` groups in flight

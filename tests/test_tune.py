@@ -56,3 +56,22 @@ def test_per_kernel_shared_memory():
     assert measured == [Config("compact", 256, False)]
     assert r.best == Config("compact", 256, False)
     assert [c.kernel for c, v in r.table if v is None] == ["pipelined", "plain"]
+
+
+def test_generated_candidates_carry_tiles_and_small_groups():
+    """The generated variant is tuned over its register tile and runs groups
+    of at most 32 cells; the table-driven kernels have no tile."""
+    smem = {"generated": 0, "compact": 105, "pipelined": 210, "plain": 210}
+    cs = candidates(smem, group_sizes=(16, 32, 64), kernels=("generated", "compact"), persistent=(True,),
+                    tiles=(4, 6, 8))
+    gen = [c for c in cs if c.kernel == "generated"]
+    assert sorted({c.tile for c in gen}) == [4, 6, 8]
+    assert {c.tile for c in cs if c.kernel == "compact"} == {6}
+    assert not fits(smem, 64, "generated") and fits(smem, 32, "generated")
+
+    def measure(c):
+        return 100.0 + c.tile if c.kernel == "generated" else 50.0
+
+    r = autotune(measure, smem, cs)
+    assert r.best == Config("generated", 16, True, 8)
+    assert [c for c, v in r.table if v is None] == [c for c in gen if c.group_size == 64]
