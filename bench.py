@@ -43,8 +43,11 @@ METRIC = "cell-intervals/s at rtol=1e-3 on 1 GB300 vs plain GPU + CPU ref; adjoi
 # `bench.py --kernel compact --steps 2 --warmup 3 --no-cpu --e2e-steps 0
 # --plain-steps 0` (3.590 TB over 0.799 PFLOP; the traffic is dominated by the
 # elimination's U operands, 8 bytes per 2-FLOP update, so it scales with the
-# FLOPs). A variant without a calibration reports no traffic.
-DRAM_BYTES_PER_FLOP = {"compact": 4.491}
+# FLOPs). generated: the two timed launches of `bench.py --cells 8192 --steps 2
+# --warmup 3 --no-cpu --e2e-steps 0 --plain-steps 0 --no-extras` (177.5 GB over
+# 99.9 GFLOP), a case small enough for the capture, scaled by the FLOPs. A
+# variant without a calibration reports no traffic.
+DRAM_BYTES_PER_FLOP = {"compact": 4.491, "generated": 1.777}
 # the integrator kernel of each variant, as ncu names it
 KERNEL_NAME = {"generated": "fo_generated_solve_kernel"}
 
@@ -391,8 +394,8 @@ def run_ours(args, rank, world):
                                  if args.kernel in DRAM_BYTES_PER_FLOP else None),
                      "traffic_unit": "bytes per launch",
                      "traffic_source": (f"ncu DRAM bytes per algorithmic FLOP of this kernel on this workload "
-                                        f"({DRAM_BYTES_PER_FLOP[args.kernel]} B/FLOP) times this run's FLOPs "
-                                        "per launch" if args.kernel in DRAM_BYTES_PER_FLOP else
+                                        f"({DRAM_BYTES_PER_FLOP[args.kernel]} B/FLOP, measured on an 8,192-cell case) "
+                                        "times this run's FLOPs per launch" if args.kernel in DRAM_BYTES_PER_FLOP else
                                         "not calibrated for this kernel variant"),
                      "kernel": KERNEL_NAME.get(args.kernel, "solve_kernel"),
                      "kernel_ms_per_launch": sum(solve_ms) / len(solve_ms),

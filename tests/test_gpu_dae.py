@@ -48,7 +48,9 @@ def test_rodas3_projection_matches_reference(cuda, case, kernel):
     assert np.all((extra[jac_lu_solve] >= 0) & (extra[jac_lu_solve] <= ties)), (got, ref)
     assert extra[4] == extra[5] == extra[6]
     assert mem.h_next == f["memory"][0]
-    assert rel_err(Y, f["Y"], floor=1e-300 + np.abs(f["atol"]).max() * 1e-4).max() <= 1e-9
+    worst = rel_err(Y, f["Y"], floor=1e-300 + np.abs(f["atol"]).max() * 1e-4).max()
+    print(f"{case} {kernel}: largest state difference {worst:.3e}")
+    assert worst <= 1e-9
 
 
 @pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact", "generated"])
@@ -71,4 +73,6 @@ def test_constrained_synthetic_matches_reference(cuda, kernel):
         st.append(int(b.status.cpu().numpy()[0]))
     assert st == list(f["status"])
     np.testing.assert_array_equal(b.counts.cpu().numpy()[0], f["counts"])
-    assert rel_err(b.state(), f["Y"]).max() <= 1e-9
+    worst = rel_err(b.state(), f["Y"]).max()
+    print(f"constrained 160x340 {kernel}: largest state difference {worst:.3e}")
+    assert worst <= 1e-9

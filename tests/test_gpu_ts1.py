@@ -28,6 +28,7 @@ def test_ts1_tier1_counts_match_the_archive(cuda, kernel):
     np.testing.assert_array_equal(total, f["counts"])
     assert total[0] == 334 and total[1] == 330 and total[2] == 4
     err = rel_err(b.state(), f["Y"])
+    print(f"TS1 {kernel}: largest state difference {err.max():.3e}")
     assert err.max() <= 1e-8, err.max()
 
 
@@ -60,7 +61,9 @@ def test_ts1_controller_variants_and_restarting_loop(cuda, variant):
     for i in range(int(f["intervals"])):
         b.step(torch.from_numpy(np.ascontiguousarray(ts1_k(f, i).T)).cuda(), float(f["dt"]), atol, float(rtol))
     np.testing.assert_array_equal(b.counts.cpu().numpy().sum(axis=0), f[f"{key}_counts"])
-    assert rel_err(b.state(), f[f"{key}_Y"]).max() <= 1e-8
+    worst = rel_err(b.state(), f[f"{key}_Y"]).max()
+    print(f"TS1 {variant}: largest state difference {worst:.3e}")
+    assert worst <= 1e-8
 
 
 def _device_k(cuda, f):
