@@ -710,7 +710,7 @@ def run_extras(args):
     import torch
     extras = {}
     runs = {
-        "batched": (run_batched, dict(cells=1048576, steps=3, warmup=3, kernel=args.kernel, ordering=args.ordering,
+        "batched": (run_batched, dict(cells=1048576, steps=10, warmup=3, kernel=args.kernel, ordering=args.ordering,
                                       autotune=False)),
         "adjoint": (run_adjoint, dict(cells=4096, steps=60, fd_directions=4)),
         "dae": (run_dae, dict(cells=16384, steps=30, warmup=3, adjoint_intervals=5, fd_directions=4)),
