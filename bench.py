@@ -259,7 +259,8 @@ def run_ours(args, rank, world):
 
     Y0 = torch.from_numpy(inputs.Y0).to(dev)
     from fastode_gb300 import Algorithm
-    batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots, algorithm=Algorithm(kernel=args.kernel, ordering=args.ordering))
+    batch = Batch(sm.mech, Y0, group_size=32, slots=args.slots,
+                  algorithm=Algorithm(kernel=args.kernel, ordering=args.ordering, tile=args.tile))
 
     def reset(b=batch):
         b.Y.copy_(Y0.t())
@@ -332,7 +333,7 @@ def run_ours(args, rank, world):
         from fastode_gb300.batch import HostState, solve_host_intervals
         pinned_k = [torch.from_numpy(inputs.k_at(i)).pin_memory() for i in range(e2e_steps)]
         Y0h = torch.from_numpy(inputs.Y0.copy()).pin_memory()
-        alg = Algorithm(kernel=args.kernel, ordering=args.ordering)
+        alg = Algorithm(kernel=args.kernel, ordering=args.ordering, tile=args.tile)
         # (1) the overlapped host API: the state stays on the device, every
         # interval's rate constants go in and its state and statuses come out,
         # on a second stream while the device integrates
@@ -772,6 +773,8 @@ def main():
                     help="generated: the mechanism's own factorization and solves as straight-line code "
                          "(compiled when the plan is made, outside the timed region); the others are "
                          "table-driven")
+    ap.add_argument("--tile", type=int, default=6,
+                    help="generated kernel: rows and columns of the factorization's register tiles")
     ap.add_argument("--ordering", default="auto", choices=["auto", "refined", "min_fill", "min_degree", "natural"],
                     help="elimination order of the sparse LU (auto: the greedy orders refined by local search)")
     ap.add_argument("--plain-steps", type=int, default=10)
