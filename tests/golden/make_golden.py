@@ -346,6 +346,53 @@ def _subset_group(args):
             np.stack([snaps[s] for s in SUBSET_SNAPSHOTS]), np.array([mem.h_next, mem.err_prev, mem.h_prev]))
 
 
+TIGHT_INTERVALS = 20
+
+
+def _tight_group(args):
+    """One group of the parity subset through the reference at rtol = 1e-10,
+    atol = 1e-10 * a: the FP64 accuracy oracle, at intervals 10 and 20."""
+    reference, root, Y0, k0, photo, J, f, dt, n, intervals = args
+    sys.path.insert(0, reference)
+    sys.path.insert(0, root)
+    from fastode import Algorithm, Counts, ROS3
+    from fastode.chem import ChemSystem, Mechanism
+    from fastode_gb300 import synthetic as syn
+    wl = syn.plain_large(n_cells=32, intervals=1)
+    rm = Mechanism(wl.sm.species, wl.sm.reactions)
+    alg = Algorithm(ROS3, max_steps=1000000)
+    mem = alg.new_memory()
+    c = Counts()
+    Y = Y0.copy()
+    atol = np.full(n, 1e-10 * 1e-14)
+    snaps = []
+    for i in range(intervals):
+        k = k0.copy()
+        k[:, photo] = J[None, :] * f[i][:, None]
+        Y, st = alg.solve(ChemSystem(rm, k), Y, dt, atol, 1e-10, c, mem)
+        assert st == "converged", st
+        if i + 1 in (10, 20):
+            snaps.append(Y.copy())
+    return np.stack(snaps), c.steps
+
+
+def c2_subset_tight(reference, subset):
+    """The reference's tight solve of the parity subset's cells (the accuracy
+    oracle of the measured run), one group per process."""
+    import multiprocessing as mp
+    gs = int(subset["group_size"])
+    G = len(subset["groups"])
+    jobs = [(reference, str(ROOT), subset["Y0"][j * gs:(j + 1) * gs], subset["k0"][j * gs:(j + 1) * gs],
+             subset["photo"], subset["J"], subset["f"][:, j * gs:(j + 1) * gs], float(subset["dt"]),
+             int(subset["n"]), TIGHT_INTERVALS) for j in range(G)]
+    os.environ["OMP_NUM_THREADS"] = os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    with mp.get_context("spawn").Pool(min(G, os.cpu_count() or 1)) as pool:
+        res = pool.map(_tight_group, jobs)
+    return dict(tight_snapshots=np.array([10, 20]),
+                Y_tight=np.stack([r[0] for r in res], axis=1).reshape(2, -1, int(subset["n"])),
+                tight_steps=np.array([r[1] for r in res]))
+
+
 def c2_subset(reference):
     """The reference on the seeded parity subset of the 210/500, 65,536-cell
     workload (synthetic.PLAIN_LARGE_PARITY_GROUPS, eight whole groups) over
@@ -397,7 +444,8 @@ def c2_subset(reference):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["backward-euler", "c2-subset", "ts1-rate-laws"], default=None,
+    ap.add_argument("--only", choices=["backward-euler", "c2-subset", "c2-subset-tight", "ts1-rate-laws"],
+                    default=None,
                     help="regenerate one fixture instead of all")
     a = ap.parse_args()
     sys.path.insert(0, a.reference)
@@ -411,13 +459,21 @@ def main():
     if a.only == "ts1-rate-laws":
         np.savez_compressed(HERE / "ts1_rate_laws.npz", **ts1_rate_laws(a.reference))
         return
+    if a.only == "c2-subset-tight":
+        sub = dict(np.load(HERE / "ros3_210x500_subset.npz"))
+        sub.update(c2_subset_tight(a.reference, sub))
+        np.savez_compressed(HERE / "ros3_210x500_subset.npz", **sub)
+        print("tight steps per group", sub["tight_steps"].tolist())
+        return
     if a.only == "c2-subset":
         out = c2_subset(a.reference)
+        out.update(c2_subset_tight(a.reference, out))
         np.savez_compressed(HERE / "ros3_210x500_subset.npz", **out)
         print("ros3_210x500_subset counts", out["counts"][:, -1].sum(axis=0).tolist(), "attempts",
               out["n_attempts"].tolist())
         return
     out = c2_subset(a.reference)
+    out.update(c2_subset_tight(a.reference, out))
     np.savez_compressed(HERE / "ros3_210x500_subset.npz", **out)
     np.savez_compressed(HERE / "ts1_rate_laws.npz", **ts1_rate_laws(a.reference))
     np.savez_compressed(HERE / "ts1_tier1_30s_backward_euler.npz", **backward_euler_ts1(a.reference))

@@ -15,6 +15,11 @@ from golden_cases import DAE_CASES, TableMechanism, load, rel_err
 
 pytestmark = pytest.mark.gpu
 
+# States within 1e-10 relative: the largest difference measured on a GB300 is
+# 5.2e-15 (tropospheric) and 8.2e-16 (constrained 160x340), roundoff of the
+# summation order.
+STATE_TOL = 1e-10
+
 
 @pytest.mark.parametrize("case", DAE_CASES)
 @pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact", "generated"])
@@ -50,7 +55,7 @@ def test_rodas3_projection_matches_reference(cuda, case, kernel):
     assert mem.h_next == f["memory"][0]
     worst = rel_err(Y, f["Y"], floor=1e-300 + np.abs(f["atol"]).max() * 1e-4).max()
     print(f"{case} {kernel}: largest state difference {worst:.3e}")
-    assert worst <= 1e-9
+    assert worst <= STATE_TOL
 
 
 @pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact", "generated"])
@@ -58,7 +63,7 @@ def test_constrained_synthetic_matches_reference(cuda, kernel):
     """The constrained synthetic workload (150 differential + 10 quasi-steady
     species, one group of 32 cells, four 60 s intervals, RODAS3 at rtol 1e-4):
     the reference's Counts (projection passes and line-search trials included)
-    and statuses; states within 1e-9 relative."""
+    and statuses; states within 1e-10 relative."""
     from golden_cases import mechanism_of
     from fastode_gb300.batch import Batch
     from fastode_gb300 import RODAS3, Algorithm
@@ -75,4 +80,4 @@ def test_constrained_synthetic_matches_reference(cuda, kernel):
     np.testing.assert_array_equal(b.counts.cpu().numpy()[0], f["counts"])
     worst = rel_err(b.state(), f["Y"]).max()
     print(f"constrained 160x340 {kernel}: largest state difference {worst:.3e}")
-    assert worst <= 1e-9
+    assert worst <= STATE_TOL

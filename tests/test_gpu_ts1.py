@@ -12,7 +12,15 @@ from golden_cases import load, rel_err, table_mechanism, ts1_k
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact"])
+# States within 1e-10 relative (floor a = 1e-14): the Counts and step sequences
+# are the reference's, and what remains is roundoff of different summation
+# orders (the reference's BLAS forcing and dense LU, the device's CSR sums and
+# sparse LU) carried through 334 steps of a stiff system; the largest measured
+# on a GB300 is 2.5e-11 (alg-nomemory), 1.8e-11 for the default controller.
+STATE_TOL = 1e-10
+
+
+@pytest.mark.parametrize("kernel", ["pipelined", "plain", "compact", "generated"])
 def test_ts1_tier1_counts_match_the_archive(cuda, kernel):
     from fastode_gb300 import Algorithm
     from fastode_gb300.batch import Batch
@@ -29,7 +37,7 @@ def test_ts1_tier1_counts_match_the_archive(cuda, kernel):
     assert total[0] == 334 and total[1] == 330 and total[2] == 4
     err = rel_err(b.state(), f["Y"])
     print(f"TS1 {kernel}: largest state difference {err.max():.3e}")
-    assert err.max() <= 1e-8, err.max()
+    assert err.max() <= STATE_TOL, err.max()
 
 
 VARIANTS = {
@@ -63,7 +71,7 @@ def test_ts1_controller_variants_and_restarting_loop(cuda, variant):
     np.testing.assert_array_equal(b.counts.cpu().numpy().sum(axis=0), f[f"{key}_counts"])
     worst = rel_err(b.state(), f[f"{key}_Y"]).max()
     print(f"TS1 {variant}: largest state difference {worst:.3e}")
-    assert worst <= 1e-8
+    assert worst <= STATE_TOL
 
 
 def _device_k(cuda, f):
@@ -125,4 +133,6 @@ def test_ts1_with_device_rate_constants_reproduces_the_archive(cuda, kernel):
     total = b.counts.cpu().numpy().sum(axis=0)
     np.testing.assert_array_equal(total, f["counts"])
     assert total[0] == 334 and total[1] == 330 and total[2] == 4
-    assert rel_err(b.state(), f["Y"]).max() <= 1e-8
+    worst = rel_err(b.state(), f["Y"]).max()
+    print(f"TS1 device rate constants {kernel}: largest state difference {worst:.3e}")
+    assert worst <= STATE_TOL
