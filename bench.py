@@ -220,6 +220,18 @@ class PlainInputs:
             got = Y[np.asarray(f["cells"])]
             out["state_max_rel"] = float((np.abs(got - ref) / np.maximum(np.abs(ref), 1e-14)).max())
             out["state_rtol"] = 1e-10
+        tight = list(np.asarray(f["tight_snapshots"])) if "tight_snapshots" in f else []
+        if intervals in tight and intervals in snaps:
+            # accuracy: Sandu digits (device scoring kernel) of the measured
+            # run and of the reference's own rtol = 1e-3 run against the
+            # reference at rtol = 1e-10, atol = 1e-10 * a on these cells
+            from fastode_gb300.scenario import digits
+            t = f["Y_tight"][tight.index(intervals)]
+            got = Y[np.asarray(f["cells"])]
+            d_dev = digits(got, t, 1e-14)[0]
+            d_ref = digits(f["Y_snap"][snaps.index(intervals)], t, 1e-14)[0]
+            out["accuracy"] = {"against": "the reference's Algorithm(ROS3) at rtol 1e-10, atol 1e-10 * a",
+                               "digits": d_dev, "reference_digits": d_ref, "difference": abs(d_dev - d_ref)}
         return out
 
 

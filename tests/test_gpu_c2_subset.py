@@ -15,7 +15,10 @@ exactly the reference's k. The bar:
   * every error norm: within 1e-8 relative plus 1e-7 absolute (the LUs differ
     in roundoff: SuperLU pivots, the device factors pivot-free);
   * states at intervals 10, 20 and 30: within STATE_RTOL relative, floored at
-    a = 1e-14.
+    a = 1e-14;
+  * accuracy: the device's Sandu digits against the reference's own FP64
+    rtol = 1e-10, atol = 1e-10 * a solve of the same cells (intervals 10 and
+    20) equal the reference's rtol = 1e-3 digits to 1e-6.
 """
 import numpy as np
 import pytest
@@ -169,6 +172,14 @@ def test_subset_matches_reference(cuda, kernel):
     worst = {s: float(rel_err(snaps[s], f["Y_snap"][j]).max()) for j, s in enumerate(f["snapshots"])}
     print(f"{kernel}: largest state difference by interval {worst}")
     assert max(worst.values()) <= STATE_RTOL, worst
+    from fastode_gb300.scenario import digits
+    snaps_ref = list(f["snapshots"])
+    for j, s in enumerate(f["tight_snapshots"]):
+        d_dev = digits(snaps[int(s)], f["Y_tight"][j], 1e-14)[0]
+        d_ref = digits(f["Y_snap"][snaps_ref.index(s)], f["Y_tight"][j], 1e-14)[0]
+        print(f"{kernel}: digits against the rtol 1e-10 solve after {int(s)} intervals: {d_dev:.6f} "
+              f"(reference {d_ref:.6f})")
+        assert abs(d_dev - d_ref) <= 1e-6 and d_ref > 4.0, (s, d_dev, d_ref)
 
 
 def test_subset_queue_and_block_per_group_agree(cuda):

@@ -271,3 +271,35 @@ def test_oracle_score_reproduces_archived_digits(state):
     assert round(D, 4) == float(row["digits"])
     assert ws == row["worst_species"] and round(wd, 4) == float(row["worst_digits"])
     assert (str(gate), str(l2), str(l3)) == (row["gate"], row["level2"], row["level3"])
+
+
+def test_oracle_reproduces_the_measured_workload_subset():
+    """The oracle on the measured 210-species / 500-reaction workload's parity
+    subset (tests/golden/ros3_210x500_subset.npz, the reference run on eight
+    seeded groups of the 65,536 cells): the first two intervals from the
+    initial state, every group. Counts, statuses, every attempted step size
+    and error norm bit for bit: the same NumPy and SciPy operations on the
+    same inputs, with BLAS on one thread as the fixture was made (more
+    threads block the forcing's matrix product differently, which moves the
+    norms by up to 5e-9 relative)."""
+    threadpoolctl = pytest.importorskip("threadpoolctl")
+    f = load("ros3_210x500_subset")
+    mech = mechanism_of(f)
+    gs = int(f["group_size"])
+    intervals = 2
+
+    def k_of(i):
+        k = np.array(f["k0"], copy=True)
+        k[:, f["photo"]] = f["J"][None, :] * f["f"][i][:, None]
+        return k
+
+    with threadpoolctl.threadpool_limits(1):
+        Y, counts, statuses, mems, traces = O.run_groups(
+            mech, f["Y0"], k_of, float(f["dt"]), intervals, f["atol"], float(f["rtol"]), group_size=gs, trace=True)
+    for g in range(len(f["groups"])):
+        assert counts[g].as_tuple() == tuple(f["counts"][g, intervals - 1])
+        assert [STATUS.index(s) for s in statuses[g]] == list(f["status"][g, :intervals])
+        na = int((f["interval_of"][g, : int(f["n_attempts"][g])] < intervals).sum())
+        assert len(traces[g]) == na
+        assert [t[1] for t in traces[g]] == list(f["hs"][g, :na])
+        assert [t[2] for t in traces[g]] == list(f["errs"][g, :na])
