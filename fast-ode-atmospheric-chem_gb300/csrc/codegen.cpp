@@ -23,8 +23,12 @@
 //
 // The solves: blocks of `solve_block` rows; each row sums its terms in
 // ascending column order, as the plain variant's loops do, so results match
-// that variant bit for bit; a solution value used by several rows of a block
-// is loaded once for the block. The transposed solve of the adjoint follows
+// that variant bit for bit. In the forward solve a solution value used by
+// several rows of a block is loaded once for the block; in the backward
+// solve the `solve_keep` values of later blocks used by most rows stay in
+// registers for the block and the rest are loaded at each use (holding all of
+// them made the register allocator spill about 47 KB per solve to local
+// memory, which missed every cache). The transposed solve of the adjoint follows
 // the same pattern with rows and columns exchanged.
 #include "codegen.h"
 
@@ -239,7 +243,7 @@ void emit_factor(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pat
   }
 }
 
-void emit_solve(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pattern& P, int b) {
+void emit_solve(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pattern& P, int b, int keep) {
   const int n = t.n;
   const int nb = (n + b - 1) / b;
   std::vector<int> xv(n, -1);   // registers of solution values finished in this block
@@ -265,9 +269,24 @@ void emit_solve(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Patt
       x.store(sl.xs + i, acc[i - i0]);
     }
   }
-  // backward: x_r = (x_r - sum over j > r of U(r, j) x_j) / pivot, ascending j
+  // backward: x_r = (x_r - sum over j > r of U(r, j) x_j) / pivot, ascending j.
+  // A row's in-block terms come before its terms in later blocks, so the
+  // later blocks' values x_j cannot be summed ahead for the whole block; the
+  // `keep` values used by most rows of the block stay in registers from their
+  // first load to the end of the block, the others are loaded at each use
+  // (keeping every one would hold up to n values live and spill them).
   for (int ib = nb - 1; ib >= 0; --ib) {
     const int i0 = ib * b, i1 = std::min(n, i0 + b);
+    std::vector<int> uses(n, 0);
+    for (int r = i0; r < i1; ++r)
+      for (int q = t.lu_diag[r] + 1; q < t.lu_row_ptr[r + 1]; ++q)
+        if (t.lu_col[q] >= i1) ++uses[t.lu_col[q]];
+    std::vector<int> order;
+    for (int j = i1; j < n; ++j)
+      if (uses[j] > 1) order.push_back(j);
+    std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return uses[u] > uses[v]; });
+    std::vector<char> kept(n, 0);
+    for (size_t m = 0; m < order.size() && (int)m < keep; ++m) kept[order[m]] = 1;
     std::vector<int> ext(n, -1);
     for (int r = i1 - 1; r >= i0; --r) {
       int acc = x.load(sl.xs + r);
@@ -276,9 +295,11 @@ void emit_solve(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Patt
         int xj;
         if (j < i1) {
           xj = xv[j];
-        } else {
+        } else if (kept[j]) {
           if (ext[j] < 0) ext[j] = x.load(sl.xs + j);
           xj = ext[j];
+        } else {
+          xj = x.load(sl.xs + j);
         }
         acc = x.fma(x.neg(x.load(sl.lu + q)), xj, acc);
       }
@@ -376,8 +397,8 @@ std::string generate_ptx(const std::vector<const HostTables*>& ts, const std::ve
                          int64_t* fma_count) {
   if (ts.empty() || os.size() != ts.size()) throw std::invalid_argument("one set of options per mechanism");
   for (const GenOptions& o : os)
-    if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64)
-      throw std::invalid_argument("tile sizes out of range");
+    if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64 || o.solve_keep < 0)
+      throw std::invalid_argument("generation options out of range");
   Ptx f, s, st;
   std::vector<std::string> fb, sb, tb;
   int64_t total = 0;
@@ -392,7 +413,7 @@ std::string generate_ptx(const std::vector<const HostTables*>& ts, const std::ve
     total += nfma;
     fb.push_back(std::move(f.body));
     f.body.clear();
-    emit_solve(s, *t, sl, P, o.solve_block);
+    emit_solve(s, *t, sl, P, o.solve_block, o.solve_keep);
     sb.push_back(std::move(s.body));
     s.body.clear();
     emit_solve_t(st, *t, sl, P, o.solve_block);

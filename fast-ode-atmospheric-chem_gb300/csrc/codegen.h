@@ -18,6 +18,8 @@ struct GenOptions {
   int tile = 6;
   // rows of a block of the triangular solves
   int solve_block = 8;
+  // values of later blocks the backward solve keeps in registers per block
+  int solve_keep = 16;
 };
 
 // PTX (ISA 9.0, sm_103a) defining
