@@ -51,7 +51,7 @@ class Options(C.Structure):
                 ("max_steps", C.c_int32), ("variant", C.c_int32), ("loop", C.c_int32),
                 ("step_change_rows", C.c_int32),
                 ("max_iterations", C.c_int32), ("nreductions", C.c_int32),
-                ("reductions", C.c_double * 8), ("small", C.c_double)]
+                ("reductions", C.c_double * 8), ("small", C.c_double), ("lockstep", C.c_int32)]
 
 
 VARIANTS = {"pipelined": 0, "plain": 1, "compact": 2, "generated": 3}

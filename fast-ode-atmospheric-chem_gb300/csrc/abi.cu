@@ -109,6 +109,7 @@ size_t smem_bytes(const fo::HostTables& t, int lanes, int variant = FO_VARIANT_P
 }
 
 constexpr size_t kHeader = 256;  // queue counter at the start of the workspace
+constexpr size_t kRoundsOffset = 64;  // the lockstep barrier words, inside the header
 constexpr int kMaxLanes = 256;
 
 template <typename T>
@@ -497,6 +498,15 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(queue)");
   } else {
     p.queue = nullptr;
+  }
+  // lockstep rounds (fo_options.lockstep): four barrier words in the
+  // workspace header, zeroed for every launch
+  p.rounds = nullptr;
+  if (opt->lockstep && p.o.variant == FO_VARIANT_GENERATED && slots <= 0 && p.o.loop == FO_LOOP_ALGORITHM &&
+      !plan->dev.has_constraints) {
+    p.rounds = reinterpret_cast<unsigned int*>(static_cast<char*>(workspace) + kRoundsOffset);
+    e = cudaMemsetAsync(p.rounds, 0, 4 * sizeof(unsigned int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(rounds)");
   }
   if (p.o.variant == FO_VARIANT_GENERATED) e = fo::gen_launch(plan->gen, p, grid, smem, s);
   else e = fo::launch_solve(p, grid, smem, s);

@@ -106,6 +106,7 @@ struct SolveParams {
   double* trace;
   int trace_cap;
   int32_t* trace_len;
+  unsigned int* rounds;          // lockstep rounds (four barrier words), or null
 };
 
 // Extra per-lane scratch of the adjoint (items after the forward layout).

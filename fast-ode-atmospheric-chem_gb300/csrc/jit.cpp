@@ -301,6 +301,14 @@ cudaError_t gen_launch(GenModule* m, const SolveParams& p, int grid, size_t smem
   if (e != cudaSuccess) return e;
   SolveParams q = p;
   void* args[] = {&q};
+  if (q.rounds != nullptr) {
+    // lockstep rounds need every block resident: a cooperative launch, which
+    // the runtime refuses when the grid does not fit; then run without rounds
+    e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32), args, smem, stream);
+    if (e != cudaErrorCooperativeLaunchTooLarge && e != cudaErrorNotSupported) return e;
+    (void)cudaGetLastError();
+    q.rounds = nullptr;
+  }
   return cudaLaunchKernel(fn, dim3(grid), dim3(32), args, smem, stream);
 }
 

@@ -1154,6 +1154,53 @@ __device__ __noinline__ void solve_group_backward_euler(const SolveParams& p, in
   }
 }
 
+// Lockstep rounds. With every group of the launch resident at once (a
+// cooperative launch), the groups make their attempts in rounds: each group
+// makes one attempt, then waits at a grid-wide barrier for the others; a
+// group that has finished keeps arriving with nothing to do until a round in
+// which no group attempted. The straight-line factorization is megabytes of
+// code, so warps that drift apart each stream their own instructions and
+// thrash the SM's instruction cache; rounds keep the warps of an SM at the
+// same place. The barrier only orders time: no group reads another's data, so
+// results are those of the unsynchronized launch bit for bit. Each wait is
+// bounded (kRoundSpinLimit polls about 4 us apart, some 30 s); a wait that
+// gives up returns -1 and the group continues without rounds.
+constexpr long long kRoundSpinLimit = 7500000;
+
+// Arrive with this group's activity in the round (1: it attempted); returns
+// the number of groups that attempted in the round, or -1. Barrier words:
+// [0] arrivals, [1] activity sum, [2] generation, [3] the last round's sum.
+// Every thread of the block calls this.
+__device__ int round_barrier(unsigned int* w, int active) {
+  __shared__ int result;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vw = w;
+    const unsigned int gen = vw[2];
+    __threadfence();
+    atomicAdd(w + 1, (unsigned int)active);
+    __threadfence();
+    if (atomicAdd(w, 1u) + 1u == gridDim.x) {
+      const unsigned int total = atomicExch(w + 1, 0u);
+      atomicExch(w + 3, total);
+      atomicExch(w, 0u);
+      __threadfence();
+      atomicAdd(w + 2, 1u);
+      result = (int)total;
+    } else {
+      long long spins = 0;
+      while (vw[2] == gen && spins < kRoundSpinLimit) {
+        __nanosleep(4000);
+        ++spins;
+      }
+      __threadfence();
+      result = vw[2] == gen ? -1 : (int)vw[3];
+    }
+  }
+  __syncthreads();
+  return result;
+}
+
 __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, double* w, double* red);
 
 __device__ void solve_group(const SolveParams& p, int g, double* scr, double* w, double* red) {
@@ -1177,6 +1224,7 @@ __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, 
 
   long long c_steps = 0, c_acc = 0, c_rej = 0, c_rhs = 0, c_jac = 0, c_lu = 0, c_solves = 0;
   int nrec = 0;
+  bool rounds = p.rounds != nullptr;
 
   double* Y = scr + p.sl.y * L;
   double* Ynew = scr + p.sl.ynew * L;
@@ -1298,6 +1346,7 @@ __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, 
         if (last) H = __dsub_rn(dt, t);
         ++c_rej;
       }
+      if (rounds) rounds = round_barrier(p.rounds, 1) >= 0;
     }
   }
   if (status < 0) status = FO_STATUS_CONVERGED;
@@ -1329,6 +1378,9 @@ __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, 
     cn[12] += 1;
     p.status[g] = status;
     if (p.trace_len) p.trace_len[g] = nrec;
+  }
+  // finished: arrive with nothing to do until a round in which no group attempted
+  while (rounds && round_barrier(p.rounds, 0) > 0) {
   }
 }
 

@@ -125,8 +125,9 @@ class Algorithm:
     def __init__(self, tableau: Tableau = ROS3, controller: str = "h211b", b: float = 4.0,
                  safety: float = 0.9, fac_min: float = 0.2, fac_max: float = 6.0,
                  carry: bool = True, quantize: bool = True, max_steps: int = 1000,
-                 carry_memory: bool = True, ordering: str = "auto", kernel: str = "generated", tile: int = 6):
-        """The reference's arguments, plus two of the device path: the
+                 carry_memory: bool = True, ordering: str = "auto", kernel: str = "generated", tile: int = 6,
+                 lockstep: bool = True):
+        """The reference's arguments, plus those of the device path: the
         fill-reducing ``ordering`` of the sparse LU and the ``kernel`` variant:
         "generated", the mechanism's own factorization and solves generated as
         straight-line code when its plan is first used (compiled once, then
@@ -136,7 +137,10 @@ class Algorithm:
         "plain", the direct loops. All give the same factors; "generated" and
         "plain" give the same solutions bit for bit, the others differ in the
         solves' summation order. ``tile``: the generated factorization's
-        register tiles (rows and columns), a speed choice only."""
+        register tiles (rows and columns), a speed choice only. ``lockstep``:
+        with the generated kernel and one block per group, the groups make
+        their attempts in rounds in a cooperative launch (fo_options.lockstep),
+        also a speed choice only."""
         self.tableau = tableau
         self.controller = controller
         self.b = b
@@ -152,6 +156,7 @@ class Algorithm:
             raise ValueError(f"kernel must be one of {sorted(_abi.VARIANTS)}")
         self.kernel = kernel
         self.tile = int(tile)
+        self.lockstep = bool(lockstep)
         tableau_id(tableau)
 
     def new_memory(self) -> Memory:
@@ -171,7 +176,8 @@ class Algorithm:
         return _abi.Options(tableau_id(self.tableau), 0 if self.controller == "h211b" else 1,
                             float(self.b), float(self.safety), float(self.fac_min), float(self.fac_max),
                             int(bool(self.carry)), int(bool(self.quantize)), int(bool(self.carry_memory)),
-                            int(self.max_steps), _abi.VARIANTS[self.kernel], 0, 0)
+                            int(self.max_steps), _abi.VARIANTS[self.kernel], 0, 0,
+                            lockstep=int(getattr(self, "lockstep", False)))
 
     def solve(self, system, Y, dt, atol, rtol, counts: Counts, memory: Memory = None):
         """Integrate one group (all rows of Y) over one interval; returns

@@ -119,3 +119,65 @@ def test_generated_constrained_systems(cuda, case):
     np.testing.assert_array_equal(out[0].state(), out[1].state())
     np.testing.assert_array_equal(out[0].counts.cpu().numpy(), out[1].counts.cpu().numpy())
     np.testing.assert_array_equal(out[0].status.cpu().numpy(), out[1].status.cpu().numpy())
+
+
+def _subset_run(cuda, f, lockstep, intervals, trace=True):
+    from fastode_gb300 import Algorithm, _abi
+    from fastode_gb300.batch import Batch
+    torch = cuda
+    b = Batch(mechanism_of(f), f["Y0"], group_size=32, trace_cap=64 if trace else 0,
+              algorithm=Algorithm(kernel="generated", lockstep=lockstep))
+    atol = torch.from_numpy(f["atol"]).cuda()
+    k = torch.from_numpy(np.ascontiguousarray(f["k0"].T)).cuda()
+    rxn = torch.from_numpy(f["photo"].astype(np.int32)).cuda()
+    J = torch.from_numpy(f["J"]).cuda()
+    fac = torch.from_numpy(np.ascontiguousarray(f["f"])).cuda()
+    traces = []
+    for i in range(intervals):
+        _abi.check(_abi.lib().fo_photolysis_factor(b.C, rxn.numel(), rxn.data_ptr(), J.data_ptr(),
+                                                   fac[i].data_ptr(), k.data_ptr(), 1, b.C, None),
+                   "fo_photolysis_factor")
+        b.step(k, float(f["dt"]), atol, float(f["rtol"]))
+        if trace:
+            tl, tr = b.trace_len.cpu().numpy(), b.trace.cpu().numpy()
+            traces.append([tr[g, : tl[g]].copy() for g in range(b.ngroups)])
+    torch.cuda.synchronize()
+    return b, traces
+
+
+def test_lockstep_rounds_give_the_same_bits(cuda):
+    """Attempts in lockstep rounds (a cooperative launch with a grid-wide
+    barrier after every attempt, fo_options.lockstep) against the same
+    integration without rounds, on the measured workload's parity subset over
+    its first 12 intervals (12 to 26 attempts per group in the first): states,
+    Counts, memory, statuses and every attempt's step size and error norm."""
+    f = load("ros3_210x500_subset")
+    a, ta = _subset_run(cuda, f, True, 12)
+    b, tb = _subset_run(cuda, f, False, 12)
+    np.testing.assert_array_equal(a.state(), b.state())
+    for x, y in ((a.counts, b.counts), (a.memory, b.memory), (a.status, b.status)):
+        np.testing.assert_array_equal(x.cpu().numpy(), y.cpu().numpy())
+    for ia, ib in zip(ta, tb):
+        for ga, gb in zip(ia, ib):
+            np.testing.assert_array_equal(ga, gb)
+    np.testing.assert_array_equal(a.counts.cpu().numpy(), f["counts"][:, 11])
+
+
+def test_lockstep_falls_back_when_the_groups_do_not_fit(cuda):
+    """More groups than the GPU holds at once: the cooperative launch is
+    refused and the groups run without rounds, with the same results."""
+    import torch
+    from fastode_gb300 import Algorithm, synthetic as syn
+    from fastode_gb300.batch import Batch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    wl = syn.plain_small(n_cells=32 * (16 * sms + 64), intervals=2)
+    at = torch.from_numpy(wl.atol).cuda()
+    out = []
+    for lockstep in (True, False):
+        b = Batch(wl.sm.mech, wl.cells.Y0, group_size=32, algorithm=Algorithm(kernel="generated", lockstep=lockstep))
+        for i in range(2):
+            b.step(torch.from_numpy(np.ascontiguousarray(wl.k_at(i).T)).cuda(), wl.dt, at, wl.rtol)
+        torch.cuda.synchronize()
+        out.append((b.state(), b.counts.cpu().numpy()))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
