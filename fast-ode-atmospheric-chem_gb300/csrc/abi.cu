@@ -110,6 +110,7 @@ size_t smem_bytes(const fo::HostTables& t, int lanes, int variant = FO_VARIANT_P
 
 constexpr size_t kHeader = 256;  // queue counter at the start of the workspace
 constexpr size_t kRoundsOffset = 64;  // the lockstep barrier words, inside the header
+constexpr int kRoundsWords = 8;
 constexpr int kMaxLanes = 256;
 
 template <typename T>
@@ -435,6 +436,7 @@ struct fo_multi {
   int32_t* d_queue = nullptr;
   double* d_scratch = nullptr;
   int64_t slot_doubles = 0;
+  unsigned int* d_rounds = nullptr;      // lockstep rounds' barrier words, or null
 };
 
 namespace {
@@ -499,13 +501,14 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   } else {
     p.queue = nullptr;
   }
-  // lockstep rounds (fo_options.lockstep): four barrier words in the
-  // workspace header, zeroed for every launch
+  // lockstep rounds (fo_options.lockstep): barrier words in the workspace
+  // header, zeroed for every launch
   p.rounds = nullptr;
-  if (opt->lockstep && p.o.variant == FO_VARIANT_GENERATED && slots <= 0 && p.o.loop == FO_LOOP_ALGORITHM &&
+  p.round_attempts = 1;
+  if (opt->lockstep && p.o.variant == FO_VARIANT_GENERATED && p.o.loop == FO_LOOP_ALGORITHM &&
       !plan->dev.has_constraints) {
     p.rounds = reinterpret_cast<unsigned int*>(static_cast<char*>(workspace) + kRoundsOffset);
-    e = cudaMemsetAsync(p.rounds, 0, 4 * sizeof(unsigned int), s);
+    e = cudaMemsetAsync(p.rounds, 0, kRoundsWords * sizeof(unsigned int), s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(rounds)");
   }
   if (p.o.variant == FO_VARIANT_GENERATED) e = fo::gen_launch(plan->gen, p, grid, smem, s);
@@ -598,11 +601,28 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
   m->d_queue = reinterpret_cast<int32_t*>(ws);
   m->d_scratch = reinterpret_cast<double*>(ws + L.scratch_off);
   m->slot_doubles = L.items * L.lanes;
-  for (auto& p : params) {
+  // lockstep rounds when every batch asks for them, runs the generated
+  // Algorithm loop without algebraic species, and every slot is resident;
+  // each batch makes as many attempts per round as the largest mechanism's
+  // attempt costs over its own (LU and three solves), at least one
+  bool lockstep = ngen == nb;
+  int64_t cost_max = 1;
+  for (int j = 0; j < nb; ++j) {
+    const fo_batch_desc& d = b[order[j]];
+    lockstep = lockstep && d.opt.lockstep && params[j].o.loop == FO_LOOP_ALGORITHM && !d.plan->dev.has_constraints;
+    cost_max = std::max<int64_t>(cost_max, d.plan->host.lu_fma + 3 * d.plan->host.solve_fma);
+  }
+  if (lockstep) lockstep = fo::gen_resident(m->gen, true, m->grid, smem);
+  m->d_rounds = lockstep ? reinterpret_cast<unsigned int*>(ws + kRoundsOffset) : nullptr;
+  for (int j = 0; j < nb; ++j) {
+    fo::SolveParams& p = params[j];
     p.scratch = m->d_scratch;
     p.slot_doubles = m->slot_doubles;
     p.lanes = L.lanes;
     p.queue = m->d_queue;
+    p.rounds = m->d_rounds;
+    const int64_t cost = std::max<int64_t>(1, b[order[j]].plan->host.lu_fma + 3 * b[order[j]].plan->host.solve_fma);
+    p.round_attempts = (int)std::max<int64_t>(1, (cost_max + cost / 2) / cost);
   }
   e = cudaMemcpy(m->d_batches, params.data(), sizeof(fo::SolveParams) * nb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -618,9 +638,14 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
 
 int fo_multi_launch(const fo_multi* m, void* stream) {
   if (!m) return fail(FO_E_INVALID, "null argument");
+  if (m->d_rounds) {
+    cudaError_t z = cudaMemsetAsync(m->d_rounds, 0, kRoundsWords * sizeof(unsigned int),
+                                    static_cast<cudaStream_t>(stream));
+    if (z != cudaSuccess) return cuda_fail(z, "cudaMemsetAsync(rounds)");
+  }
   cudaError_t e = m->gen ? fo::gen_launch_multi(m->gen, m->d_batches, m->nb, m->d_starts, m->d_queue,
                                                 m->d_scratch, m->slot_doubles, m->grid, m->smem,
-                                                static_cast<cudaStream_t>(stream))
+                                                m->d_rounds != nullptr, static_cast<cudaStream_t>(stream))
                          : fo::launch_solve_multi(m->d_batches, m->nb, m->d_starts, m->d_queue, m->d_scratch,
                                                   m->slot_doubles, m->grid, m->lanes, m->smem,
                                                   static_cast<cudaStream_t>(stream));

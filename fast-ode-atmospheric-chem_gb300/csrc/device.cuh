@@ -106,7 +106,8 @@ struct SolveParams {
   double* trace;
   int trace_cap;
   int32_t* trace_len;
-  unsigned int* rounds;          // lockstep rounds (four barrier words), or null
+  unsigned int* rounds;          // lockstep rounds (five barrier words), or null
+  int round_attempts;            // attempts per round
 };
 
 // Extra per-lane scratch of the adjoint (items after the forward layout).

@@ -26,17 +26,18 @@ extern "C" __global__ void __launch_bounds__(32, 16) fo_generated_solve_kernel(f
   double* scr = p.scratch + (int64_t)blockIdx.x * p.slot_doubles;
   if (p.queue == nullptr) {
     fo::solve_group(p, blockIdx.x, scr, w, red);
-    return;
+  } else {
+    __shared__ int next;
+    for (;;) {
+      __syncthreads();
+      if (threadIdx.x == 0) next = atomicAdd(p.queue, 1);
+      __syncthreads();
+      const int g = next;
+      if (g >= p.ngroups) break;
+      fo::solve_group(p, g, scr, w, red);
+    }
   }
-  __shared__ int next;
-  for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) next = atomicAdd(p.queue, 1);
-    __syncthreads();
-    const int g = next;
-    if (g >= p.ngroups) break;
-    fo::solve_group(p, g, scr, w, red);
-  }
+  fo::rounds_drain(p.rounds);
 }
 
 // Several mechanisms in one persistent launch (the generated form of
@@ -51,6 +52,9 @@ extern "C" __global__ void __launch_bounds__(32, 16)
   double* w = smem + 32;
   double* scr = scratch + (int64_t)blockIdx.x * slot_doubles;
   __shared__ int next;
+  __shared__ fo::SolveParams params;
+  int current = -1;
+  unsigned int* const rounds = batches[0].rounds;   // the same words in every batch
   const int total = starts[nb];
   for (;;) {
     __syncthreads();
@@ -60,8 +64,10 @@ extern "C" __global__ void __launch_bounds__(32, 16)
     if (item >= total) break;
     int b = 0;
     while (b + 1 < nb && item >= starts[b + 1]) ++b;
-    fo::solve_group(batches[b], item - starts[b], scr, w, red);
+    fo::load_batch_params(batches, b, current, params);
+    fo::solve_group(params, item - starts[b], scr, w, red);
   }
+  fo::rounds_drain(rounds);
 }
 
 // The discrete adjoint of one interval (adjoint.cuh) on the mechanism's

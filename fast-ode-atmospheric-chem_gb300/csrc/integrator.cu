@@ -104,6 +104,8 @@ __global__ void __maxnreg__(255) solve_multi_kernel(const SolveParams* __restric
   double* w = smem + 32;
   double* scr = scratch + (int64_t)blockIdx.x * slot_doubles;
   __shared__ int next;
+  __shared__ SolveParams params;
+  int current = -1;
   const int total = starts[nb];
   for (;;) {
     __syncthreads();
@@ -113,7 +115,8 @@ __global__ void __maxnreg__(255) solve_multi_kernel(const SolveParams* __restric
     if (item >= total) break;
     int b = 0;
     while (b + 1 < nb && item >= starts[b + 1]) ++b;
-    solve_group(batches[b], item - starts[b], scr, w, red);
+    load_batch_params(batches, b, current, params);
+    solve_group(params, item - starts[b], scr, w, red);
   }
 }
 

@@ -293,7 +293,30 @@ cudaError_t ensure_smem(GenModule* m, int which, const void* fn, size_t smem) {
   return cudaSuccess;
 }
 
+// Whether `grid` one-warp blocks of kernel `fn` with `smem` bytes of dynamic
+// shared memory are all resident at once on the current device (what a
+// cooperative launch needs).
+bool all_resident(const void* fn, int grid, size_t smem) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32, smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return (int64_t)per_sm * sms >= grid;
+}
+
 }  // namespace
+
+bool gen_resident(GenModule* m, bool multi, int grid, size_t smem) {
+  const void* fn = reinterpret_cast<const void*>(multi ? m->multi_kernel : m->kernel);
+  if (ensure_smem(m, multi ? 1 : 0, fn, smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return all_resident(fn, grid, smem);
+}
 
 cudaError_t gen_launch(GenModule* m, const SolveParams& p, int grid, size_t smem, cudaStream_t stream) {
   const void* fn = reinterpret_cast<const void*>(m->kernel);
@@ -301,14 +324,11 @@ cudaError_t gen_launch(GenModule* m, const SolveParams& p, int grid, size_t smem
   if (e != cudaSuccess) return e;
   SolveParams q = p;
   void* args[] = {&q};
-  if (q.rounds != nullptr) {
-    // lockstep rounds need every block resident: a cooperative launch, which
-    // the runtime refuses when the grid does not fit; then run without rounds
-    e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32), args, smem, stream);
-    if (e != cudaErrorCooperativeLaunchTooLarge && e != cudaErrorNotSupported) return e;
-    (void)cudaGetLastError();
-    q.rounds = nullptr;
-  }
+  // lockstep rounds need every block resident: a cooperative launch; a grid
+  // that does not fit runs without rounds
+  if (q.rounds != nullptr && all_resident(fn, grid, smem))
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32), args, smem, stream);
+  q.rounds = nullptr;
   return cudaLaunchKernel(fn, dim3(grid), dim3(32), args, smem, stream);
 }
 
@@ -323,13 +343,14 @@ cudaError_t gen_launch_adjoint(GenModule* m, const AdjParams& a, int grid, size_
 
 cudaError_t gen_launch_multi(GenModule* m, const SolveParams* batches, int nb, const int32_t* starts,
                              int32_t* queue, double* scratch, int64_t slot_doubles, int grid, size_t smem,
-                             cudaStream_t stream) {
+                             bool cooperative, cudaStream_t stream) {
   const void* fn = reinterpret_cast<const void*>(m->multi_kernel);
   cudaError_t e = ensure_smem(m, 1, fn, smem);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(queue, 0, sizeof(int32_t), stream);
   if (e != cudaSuccess) return e;
   void* args[] = {&batches, &nb, &starts, &queue, &scratch, &slot_doubles};
+  if (cooperative) return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32), args, smem, stream);
   return cudaLaunchKernel(fn, dim3(grid), dim3(32), args, smem, stream);
 }
 

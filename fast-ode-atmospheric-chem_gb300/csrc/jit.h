@@ -29,9 +29,13 @@ cudaError_t gen_launch(GenModule* m, const SolveParams& p, int grid, size_t smem
 // blocks of 32 lanes.
 cudaError_t gen_launch_adjoint(GenModule* m, const AdjParams& a, int grid, size_t smem, cudaStream_t stream);
 // One persistent launch of the generated several-mechanism kernel (the
-// module made from every batch's tables, each batch's gen_index set).
+// module made from every batch's tables, each batch's gen_index set); a
+// cooperative launch when the batches run in lockstep rounds.
 cudaError_t gen_launch_multi(GenModule* m, const SolveParams* batches, int nb, const int32_t* starts,
                              int32_t* queue, double* scratch, int64_t slot_doubles, int grid, size_t smem,
-                             cudaStream_t stream);
+                             bool cooperative, cudaStream_t stream);
+// Whether `grid` blocks of the single-batch (multi false) or several-mechanism
+// kernel are all resident at once on the current device.
+bool gen_resident(GenModule* m, bool multi, int grid, size_t smem);
 
 }  // namespace fo

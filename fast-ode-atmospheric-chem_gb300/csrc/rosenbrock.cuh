@@ -1154,51 +1154,88 @@ __device__ __noinline__ void solve_group_backward_euler(const SolveParams& p, in
   }
 }
 
-// Lockstep rounds. With every group of the launch resident at once (a
-// cooperative launch), the groups make their attempts in rounds: each group
-// makes one attempt, then waits at a grid-wide barrier for the others; a
-// group that has finished keeps arriving with nothing to do until a round in
-// which no group attempted. The straight-line factorization is megabytes of
-// code, so warps that drift apart each stream their own instructions and
-// thrash the SM's instruction cache; rounds keep the warps of an SM at the
-// same place. The barrier only orders time: no group reads another's data, so
-// results are those of the unsynchronized launch bit for bit. Each wait is
-// bounded (kRoundSpinLimit polls about 4 us apart, some 30 s); a wait that
-// gives up returns -1 and the group continues without rounds.
+// Lockstep rounds. With every block of the launch resident at once (a
+// cooperative launch), the groups make their attempts in rounds: each block
+// makes one attempt (or p.round_attempts attempts, so that a round of a small
+// mechanism costs about as much as one of the largest in a several-mechanism
+// launch), then waits at a grid-wide barrier for the others; a block with no
+// group left keeps arriving with nothing to do until a round in which no
+// block attempted. The straight-line factorization is megabytes of code, so
+// warps that drift apart each stream their own instructions and thrash the
+// SM's instruction cache; rounds keep the warps of an SM at the same place
+// (the cold first interval of the 210/500, 65,536-cell job: 1.47 s without
+// rounds, 0.96 s with). The barrier only orders time: no group reads
+// another's data, so results are those of the unsynchronized launch bit for
+// bit. Each wait is bounded (kRoundSpinLimit polls about 4 us apart, some
+// 30 s); a wait that gives up raises the give-up word, after which every
+// block runs on without rounds.
 constexpr long long kRoundSpinLimit = 7500000;
 
-// Arrive with this group's activity in the round (1: it attempted); returns
-// the number of groups that attempted in the round, or -1. Barrier words:
-// [0] arrivals, [1] activity sum, [2] generation, [3] the last round's sum.
-// Every thread of the block calls this.
+// Arrive with this block's activity in the round (1: it attempted); returns
+// the number of blocks that attempted in the round, or -1 once rounds are
+// given up. Barrier words: [0] arrivals, [1] activity sum, [2] generation,
+// [3] the last round's sum, [4] give-up. Every thread of the block calls it.
 __device__ int round_barrier(unsigned int* w, int active) {
   __shared__ int result;
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int* vw = w;
-    const unsigned int gen = vw[2];
-    __threadfence();
-    atomicAdd(w + 1, (unsigned int)active);
-    __threadfence();
-    if (atomicAdd(w, 1u) + 1u == gridDim.x) {
-      const unsigned int total = atomicExch(w + 1, 0u);
-      atomicExch(w + 3, total);
-      atomicExch(w, 0u);
-      __threadfence();
-      atomicAdd(w + 2, 1u);
-      result = (int)total;
+    if (vw[4] != 0u) {
+      result = -1;
     } else {
-      long long spins = 0;
-      while (vw[2] == gen && spins < kRoundSpinLimit) {
-        __nanosleep(4000);
-        ++spins;
-      }
+      const unsigned int gen = vw[2];
       __threadfence();
-      result = vw[2] == gen ? -1 : (int)vw[3];
+      atomicAdd(w + 1, (unsigned int)active);
+      __threadfence();
+      if (atomicAdd(w, 1u) + 1u == gridDim.x) {
+        const unsigned int total = atomicExch(w + 1, 0u);
+        atomicExch(w + 3, total);
+        atomicExch(w, 0u);
+        __threadfence();
+        atomicAdd(w + 2, 1u);
+        result = (int)total;
+      } else {
+        long long spins = 0;
+        while (vw[2] == gen && vw[4] == 0u && spins < kRoundSpinLimit) {
+          __nanosleep(4000);
+          ++spins;
+        }
+        __threadfence();
+        if (vw[2] != gen) {
+          result = (int)vw[3];
+        } else {
+          atomicExch(w + 4, 1u);
+          result = -1;
+        }
+      }
     }
   }
   __syncthreads();
   return result;
+}
+
+// The parameters of batch b of a several-mechanism launch, copied from the
+// batch table in global memory into the block's shared copy when the block
+// moves to another batch, so that the integrator's parameter reads do not
+// compete with the factorization's operand stream for L1. Every thread of
+// the block calls this.
+__device__ __forceinline__ void load_batch_params(const SolveParams* __restrict__ batches, int b, int& current,
+                                                  SolveParams& shared) {
+  static_assert(sizeof(SolveParams) % sizeof(long long) == 0, "SolveParams copies as 8-byte words");
+  if (b == current) return;
+  __syncthreads();
+  const long long* src = reinterpret_cast<const long long*>(batches + b);
+  long long* dst = reinterpret_cast<long long*>(&shared);
+  for (int i = threadIdx.x; i < (int)(sizeof(SolveParams) / sizeof(long long)); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  current = b;
+}
+
+// A block with no group left: arrive idle until a round without attempts.
+__device__ __forceinline__ void rounds_drain(unsigned int* w) {
+  if (w != nullptr)
+    while (round_barrier(w, 0) > 0) {
+    }
 }
 
 __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, double* w, double* red);
@@ -1224,7 +1261,7 @@ __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, 
 
   long long c_steps = 0, c_acc = 0, c_rej = 0, c_rhs = 0, c_jac = 0, c_lu = 0, c_solves = 0;
   int nrec = 0;
-  bool rounds = p.rounds != nullptr;
+  int since_round = 0;
 
   double* Y = scr + p.sl.y * L;
   double* Ynew = scr + p.sl.ynew * L;
@@ -1346,7 +1383,10 @@ __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, 
         if (last) H = __dsub_rn(dt, t);
         ++c_rej;
       }
-      if (rounds) rounds = round_barrier(p.rounds, 1) >= 0;
+      if (p.rounds != nullptr && ++since_round >= p.round_attempts) {
+        since_round = 0;
+        round_barrier(p.rounds, 1);
+      }
     }
   }
   if (status < 0) status = FO_STATUS_CONVERGED;
@@ -1378,9 +1418,6 @@ __device__ void solve_group_algorithm(const SolveParams& p, int g, double* scr, 
     cn[12] += 1;
     p.status[g] = status;
     if (p.trace_len) p.trace_len[g] = nrec;
-  }
-  // finished: arrive with nothing to do until a round in which no group attempted
-  while (rounds && round_barrier(p.rounds, 0) > 0) {
   }
 }
 

@@ -12,14 +12,15 @@ def small_parts():
     return syn.batched_uneven(n_cells=32 * 6, intervals=4, sizes=((20, 40), (60, 40), (30, 70)))
 
 
-def make_parts(wls, cuda, kernel="generated"):
+def make_parts(wls, cuda, kernel="generated", lockstep=True):
     from fastode_gb300 import Algorithm
     from fastode_gb300.multi import Part
     parts = []
     for wl in wls:
         photo = np.nonzero(wl.sm.photolytic)[0]
         parts.append(Part(wl.sm.mech, wl.cells.Y0, wl.k_at(0), wl.atol, wl.rtol, wl.dt, group_size=32,
-                          algorithm=Algorithm(kernel=kernel), photolysis=(photo, wl.sm.J[photo], wl.cells.phase)))
+                          algorithm=Algorithm(kernel=kernel, lockstep=lockstep),
+                          photolysis=(photo, wl.sm.J[photo], wl.cells.phase)))
     return parts
 
 
@@ -89,3 +90,26 @@ def test_multi_matches_oracle_on_dark_and_lit_cells(cuda):
 def MultiBatch_from(wls, cuda):
     from fastode_gb300.multi import MultiBatch
     return MultiBatch(make_parts(wls, cuda))
+
+
+@pytest.mark.parametrize("slots", [0, 4])
+def test_multi_lockstep_rounds_give_the_same_bits(cuda, slots):
+    """Lockstep rounds in the several-mechanism launch (a cooperative launch;
+    each mechanism makes as many attempts per round as the largest one's
+    attempt costs over its own), captured in the interval graph and replayed,
+    against the same launch without rounds: every part's states, Counts,
+    memory and statuses bit for bit; with four slots for eighteen groups the
+    slots also pull further groups between rounds."""
+    from fastode_gb300.multi import MultiBatch
+    torch = cuda
+    wls = small_parts()
+    runs = []
+    for lockstep in (True, False):
+        mb = MultiBatch(make_parts(wls, cuda, lockstep=lockstep), slots=slots)
+        mb.run(4, graph=True)
+        torch.cuda.synchronize()
+        runs.append([(p.state(), p.counts.cpu().numpy(), p.memory.cpu().numpy(), p.status.cpu().numpy())
+                     for p in mb.parts])
+    for a, b in zip(*runs):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
