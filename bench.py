@@ -44,10 +44,10 @@ METRIC = "cell-intervals/s at rtol=1e-3 on 1 GB300 vs plain GPU + CPU ref; adjoi
 # --plain-steps 0` (3.590 TB over 0.799 PFLOP; the traffic is dominated by the
 # elimination's U operands, 8 bytes per 2-FLOP update, so it scales with the
 # FLOPs). generated: the two timed launches of `bench.py --cells 8192 --steps 2
-# --warmup 3 --no-cpu --e2e-steps 0 --plain-steps 0 --no-extras` (177.5 GB over
+# --warmup 3 --no-cpu --e2e-steps 0 --plain-steps 0 --no-extras` (167.3 GB over
 # 99.9 GFLOP), a case small enough for the capture, scaled by the FLOPs. A
 # variant without a calibration reports no traffic.
-DRAM_BYTES_PER_FLOP = {"compact": 4.491, "generated": 1.777}
+DRAM_BYTES_PER_FLOP = {"compact": 4.491, "generated": 1.675}
 # the integrator kernel of each variant, as ncu names it
 KERNEL_NAME = {"generated": "fo_generated_solve_kernel"}
 
@@ -472,9 +472,9 @@ def run_batched(args):
     chosen = [(32, args.kernel, 6) for _ in wls]
     tuning = None
     if args.autotune:
-        # per mechanism: group size, kernel and the generated code's register
-        # tile, measured on 4,096 of its cells (one untimed and two timed
-        # intervals each)
+        # per mechanism: group size (8 to 128 cells), kernel and the
+        # generated code's register tile, measured on 4,096 of its cells (one
+        # untimed and two timed intervals each)
         from fastode_gb300.tune import autotune, candidates, measure_on_device
         from fastode_gb300.plan import plan_for
         tiles = tuple(int(t) for t in str(getattr(args, "tune_tiles", "6")).split(","))
@@ -486,8 +486,9 @@ def run_batched(args):
             bp = plan_for(sample.sm.mech)
             smem = {k: bp.smem_items(k) for k in ("pipelined", "plain", "compact")}
             smem["generated"] = 0
-            res = autotune(measure, smem, candidates(smem, group_sizes=(16, 32), kernels=("generated", "compact"),
-                                                     persistent=(True,), tiles=tiles))
+            res = autotune(measure, smem, candidates(smem, group_sizes=(8, 16, 32, 64, 128),
+                                                     kernels=("generated", "compact"), persistent=(True,),
+                                                     tiles=tiles))
             if res.best.kernel != "generated":       # one launch runs one family of kernels
                 gen = [(c, v) for c, v in res.table if c.kernel == "generated" and v is not None]
                 best = max(gen, key=lambda cv: cv[1])[0] if gen else res.best
@@ -724,7 +725,7 @@ def run_extras(args):
     extras = {}
     runs = {
         "batched": (run_batched, dict(cells=1048576, steps=10, warmup=3, kernel=args.kernel, ordering=args.ordering,
-                                      autotune=False)),
+                                      autotune=True)),
         "adjoint": (run_adjoint, dict(cells=4096, steps=60, fd_directions=4)),
         "dae": (run_dae, dict(cells=16384, steps=30, warmup=3, adjoint_intervals=5, fd_directions=4)),
     }
