@@ -486,9 +486,12 @@ def run_batched(args):
             bp = plan_for(sample.sm.mech)
             smem = {k: bp.smem_items(k) for k in ("pipelined", "plain", "compact")}
             smem["generated"] = 0
-            res = autotune(measure, smem, candidates(smem, group_sizes=(8, 16, 32, 64, 128),
-                                                     kernels=("generated", "compact"), persistent=(True,),
-                                                     tiles=tiles))
+            # the generated kernel for groups of up to 32 cells, the compact
+            # one above (below 32 cells it measured slower than the generated)
+            cands = [c for c in candidates(smem, group_sizes=(8, 16, 32, 64, 128), kernels=("generated", "compact"),
+                                           persistent=(True,), tiles=tiles)
+                     if (c.kernel == "generated") == (c.group_size <= 32)]
+            res = autotune(measure, smem, cands)
             if res.best.kernel != "generated":       # one launch runs one family of kernels
                 gen = [(c, v) for c, v in res.table if c.kernel == "generated" and v is not None]
                 best = max(gen, key=lambda cv: cv[1])[0] if gen else res.best

@@ -505,8 +505,7 @@ int fo_solve(const fo_plan* plan, const fo_options* opt, int32_t ngroups, const 
   // header, zeroed for every launch
   p.rounds = nullptr;
   p.round_attempts = 1;
-  if (opt->lockstep && p.o.variant == FO_VARIANT_GENERATED && p.o.loop == FO_LOOP_ALGORITHM &&
-      !plan->dev.has_constraints) {
+  if (opt->lockstep && p.o.variant == FO_VARIANT_GENERATED && p.o.loop == FO_LOOP_ALGORITHM) {
     p.rounds = reinterpret_cast<unsigned int*>(static_cast<char*>(workspace) + kRoundsOffset);
     e = cudaMemsetAsync(p.rounds, 0, kRoundsWords * sizeof(unsigned int), s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(rounds)");
@@ -601,15 +600,15 @@ int fo_multi_prepare(int32_t nb, const fo_batch_desc* b, void* workspace, size_t
   m->d_queue = reinterpret_cast<int32_t*>(ws);
   m->d_scratch = reinterpret_cast<double*>(ws + L.scratch_off);
   m->slot_doubles = L.items * L.lanes;
-  // lockstep rounds when every batch asks for them, runs the generated
-  // Algorithm loop without algebraic species, and every slot is resident;
+  // lockstep rounds when every batch asks for them and runs the generated
+  // Algorithm loop, and every slot is resident;
   // each batch makes as many attempts per round as the largest mechanism's
   // attempt costs over its own (LU and three solves), at least one
   bool lockstep = ngen == nb;
   int64_t cost_max = 1;
   for (int j = 0; j < nb; ++j) {
     const fo_batch_desc& d = b[order[j]];
-    lockstep = lockstep && d.opt.lockstep && params[j].o.loop == FO_LOOP_ALGORITHM && !d.plan->dev.has_constraints;
+    lockstep = lockstep && d.opt.lockstep && params[j].o.loop == FO_LOOP_ALGORITHM;
     cost_max = std::max<int64_t>(cost_max, d.plan->host.lu_fma + 3 * d.plan->host.solve_fma);
   }
   if (lockstep) lockstep = fo::gen_resident(m->gen, true, m->grid, smem);

@@ -132,13 +132,12 @@ typedef struct fo_options {
   int32_t nreductions;        /* entries of reductions used, 0..8 (5) */
   double reductions[8];       /* step factor after the i-th failed step (0.5, 0.5, 0.5, 0.5, 0.1); each > 0 */
   double small;               /* floor of the convergence bound (1e-40) */
-  /* Nonzero: with FO_VARIANT_GENERATED, FO_LOOP_ALGORITHM, no algebraic
-   * species, one block per group (slots 0) and every group resident at once,
-   * fo_solve makes the groups' attempts in rounds (one attempt per group,
-   * then a grid-wide barrier) in a cooperative launch, which keeps the warps
-   * of an SM in the same part of the generated code. Results are the same
-   * bit for bit; otherwise, or when the launch cannot hold every group, the
-   * groups run unsynchronized. */
+  /* Nonzero: with FO_VARIANT_GENERATED and FO_LOOP_ALGORITHM, when every
+   * block of the launch is resident at once, fo_solve and fo_multi_launch
+   * make the groups' attempts in rounds (one attempt per block, then a
+   * grid-wide barrier) in a cooperative launch, which keeps the warps of an
+   * SM in the same part of the generated code. Results are the same bit for
+   * bit; otherwise the groups run unsynchronized. */
   int32_t lockstep;
 } fo_options;
 
