@@ -317,3 +317,13 @@ def test_generated_code_covers_every_update(built_library, case):
     rc, info, err = _gen_check(mechanism_of(load(case)), link=False)
     assert rc == 0, err
     assert info["ptx_bytes"] > 0
+
+
+def test_lockstep_option_reaches_fo_options():
+    """Algorithm(lockstep=...) sets fo_options.lockstep (the rounds of the
+    generated kernel are on by default, a speed choice only); the other
+    step loops keep the Algorithm value they inherit."""
+    from fastode_gb300 import Algorithm, RestartingLoop
+    assert Algorithm().options().lockstep == 1
+    assert Algorithm(lockstep=False).options().lockstep == 0
+    assert RestartingLoop().options().lockstep == 1
