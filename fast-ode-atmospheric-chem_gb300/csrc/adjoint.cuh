@@ -204,6 +204,8 @@ __device__ __noinline__ void reverse_step(const AdjParams& a, const Lane& ln, do
     lu_solve_transposed(p, ln, lu, w);                                   // w = mu_r
 #endif
     const double* Kr = K + (int64_t)r * n * L;
+    double coefs[4];                                                     // c(r, s) / h once per stage
+    for (int s = 0; s < r; ++s) coefs[s] = tb.c[r][s] / h;
     for (int i = 0; i < n; ++i) {
       const double mu = SCR(muv, i);
       const int e1 = __ldg(p.t.j_row_ptr + i + 1);
@@ -212,7 +214,7 @@ __device__ __noinline__ void reverse_step(const AdjParams& a, const Lane& ln, do
       double* Ff = Fbar + (int64_t)f * n * L;
       SCR(Ff, i) += mu;
       for (int s = 0; s < r; ++s) {
-        const double coef = tb.c[r][s] / h;
+        const double coef = coefs[s];
         if (coef != 0.0) {
           const double mv = dae ? mu * __ldg(p.t.mass + i) : mu;
           double* Ks = Kbar + (int64_t)s * n * L;

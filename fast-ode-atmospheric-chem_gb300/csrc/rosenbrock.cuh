@@ -694,10 +694,14 @@ __device__ __noinline__ double attempt(const SolveParams& p, const Lane& ln, dou
     }
     double* Kr = K + (int64_t)r * n * L;
     const bool in_place = solves_in_place(p);   // right-hand side in Kr, solved in place
+    // the stage's c(r, s) / H once per stage rather than once per species
+    // (the same quotients, so the same sums bit for bit)
+    double coefs[4];
+    for (int s = 0; s < r; ++s) coefs[s] = __ddiv_rn(tb.c[r][s], H);
     for (int i = 0; i < n; ++i) {
       double v = SCR(forcing, i);
       for (int s = 0; s < r; ++s) {
-        const double coef = __ddiv_rn(tb.c[r][s], H);
+        const double coef = coefs[s];
         if (coef != 0.0) {
           double ks = SCR(K + (int64_t)s * n * L, i);
           if (dae) ks = __dmul_rn(ks, __ldg(p.t.mass + i));
