@@ -162,11 +162,13 @@ typedef struct fo_options {
  * FO_STATUS_TOO_MANY_STEPS). */
 #define FO_LOOP_BACKWARD_EULER 2
 
-/* Kernel variants of the factorization and solves. PIPELINED streams the
+/* Kernel variants of the factorization and solves. GENERATED (below) is the
+ * fastest, for groups of up to 32 cells, and the default of the Python
+ * layer; the table-driven ones serve larger groups: PIPELINED streams the
  * elimination schedule in hazard-free chunks through a shared-memory operand
  * ring, with the whole compressed row on chip; PLAIN is the direct
  * row-by-row loop, kept as the baseline it is measured against; COMPACT
- * (below) is the fastest where its tables fit. */
+ * (below) is the fastest table-driven one where its tables fit. */
 #define FO_VARIANT_PIPELINED 0
 #define FO_VARIANT_PLAIN 1
 /* COMPACT eliminates every row in two passes over halves of its slots (the
