@@ -119,7 +119,11 @@ Pattern pattern_of(const HostTables& t) {
   return P;
 }
 
-void emit_factor(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pattern& P, int b, int64_t* nfma) {
+// Row blocks [ib_begin, ib_end) of the factorization. A row block reads the
+// entries earlier blocks stored and keeps nothing in registers past its end,
+// so consecutive ranges can be separate functions called one after another.
+void emit_factor(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pattern& P, int b, int ib_begin,
+                 int ib_end, int64_t* nfma) {
   const int n = t.n;
   // Jacobian entry (assembly order) stored at each LU position, or -1
   std::vector<int32_t> jac_at(t.lu_col.size(), -1);
@@ -127,7 +131,7 @@ void emit_factor(Ptx& x, const HostTables& t, const ScratchLayout& sl, const Pat
   const int nb = (n + b - 1) / b;
   std::vector<int> a((size_t)b * b);
   auto A = [&](int i, int j, int i0, int j0) -> int& { return a[(size_t)(i - i0) * b + (j - j0)]; };
-  for (int ib = 0; ib < nb; ++ib) {
+  for (int ib = std::max(0, ib_begin); ib < std::min(nb, ib_end); ++ib) {
     const int i0 = ib * b, i1 = std::min(n, i0 + b);
     for (int jb = 0; jb < nb; ++jb) {
       const int j0 = jb * b, j1 = std::min(n, j0 + b);
@@ -391,28 +395,82 @@ std::string function(const char* name, const char* params, const Ptx& x, const s
   return s;
 }
 
+// The factorization: every piece of every mechanism as its own function
+// (fo_gen_factor_m<m>_p<k>: base, alpha), then fo_gen_factor(base, alpha,
+// mech), which calls mechanism mech's pieces in order. Separate functions
+// keep each compilation unit of the register allocator and scheduler small.
+std::string factor_functions(const std::vector<std::vector<Ptx>>& pieces) {
+  std::string out;
+  for (size_t m = 0; m < pieces.size(); ++m)
+    for (size_t k = 0; k < pieces[m].size(); ++k) {
+      const Ptx& x = pieces[m][k];
+      const std::string name = "fo_gen_factor_m" + std::to_string(m) + "_p" + std::to_string(k);
+      out.reserve(out.size() + x.body.size() + 512);
+      out += ".func " + name + "(.param .b64 " + name + "_base, .param .b64 " + name + "_alpha)\n{\n";
+      out += "\t.reg .f64 %d<" + std::to_string(x.next + 1) + ">;\n\t.reg .b64 %p;\n\t.reg .b64 %b;\n"
+             "\t.reg .b64 %a;\n";
+      out += "\tld.param.b64 %p, [" + name + "_base];\n\tld.param.b64 %a, [" + name + "_alpha];\n"
+             "\tmov.b64 %d0, %a;\n\tcvta.to.global.u64 %b, %p;\n";
+      out += x.body;
+      out += "\tret;\n}\n\n";
+    }
+  out += ".visible .func fo_gen_factor(.param .b64 fo_gen_factor_base, .param .b64 fo_gen_factor_alpha, "
+         ".param .b32 fo_gen_factor_mech)\n{\n\t.reg .b64 %p;\n\t.reg .b64 %a;\n\t.reg .b32 %m;\n"
+         "\t.reg .pred %q;\n\tld.param.b64 %p, [fo_gen_factor_base];\n\tld.param.b64 %a, [fo_gen_factor_alpha];\n"
+         "\tld.param.b32 %m, [fo_gen_factor_mech];\n";
+  for (size_t m = 0; m < pieces.size(); ++m) {
+    const std::string label = "$fo_gen_factor_m" + std::to_string(m + 1);
+    if (m + 1 < pieces.size()) out += "\tsetp.ne.s32 %q, %m, " + std::to_string(m) + ";\n\t@%q bra " + label + ";\n";
+    for (size_t k = 0; k < pieces[m].size(); ++k)
+      out += "\t{\n\t.param .b64 fo_arg_base;\n\t.param .b64 fo_arg_alpha;\n\tst.param.b64 [fo_arg_base], %p;\n"
+             "\tst.param.b64 [fo_arg_alpha], %a;\n\tcall.uni fo_gen_factor_m" + std::to_string(m) + "_p" +
+             std::to_string(k) + ", (fo_arg_base, fo_arg_alpha);\n\t}\n";
+    out += "\tret;\n";
+    if (m + 1 < pieces.size()) out += label + ":\n";
+  }
+  out += "}\n";
+  return out;
+}
+
 }  // namespace
 
 std::string generate_ptx(const std::vector<const HostTables*>& ts, const std::vector<GenOptions>& os,
                          int64_t* fma_count) {
   if (ts.empty() || os.size() != ts.size()) throw std::invalid_argument("one set of options per mechanism");
   for (const GenOptions& o : os)
-    if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64 || o.solve_keep < 0)
+    if (o.tile < 1 || o.tile > 16 || o.solve_block < 1 || o.solve_block > 64 || o.solve_keep < 0 ||
+        o.piece_lines < 1)
       throw std::invalid_argument("generation options out of range");
-  Ptx f, s, st;
-  std::vector<std::string> fb, sb, tb;
+  Ptx s, st;
+  std::vector<std::string> sb, tb;
+  // the factorization of mechanism m: pieces[m][k] = the k-th function
+  std::vector<std::vector<Ptx>> pieces(ts.size());
   int64_t total = 0;
   for (size_t m = 0; m < ts.size(); ++m) {
     const HostTables* t = ts[m];
     const GenOptions& o = os[m];
     const ScratchLayout sl = layout_of(*t);
     const Pattern P = pattern_of(*t);
+    // consecutive row blocks up to about o.piece_lines instructions each
+    const int nb = (t->n + o.tile - 1) / o.tile;
+    std::vector<size_t> lines(nb);
+    for (int ib = 0; ib < nb; ++ib) {
+      Ptx probe;
+      int64_t ignored = 0;
+      emit_factor(probe, *t, sl, P, o.tile, ib, ib + 1, &ignored);
+      lines[ib] = (size_t)std::count(probe.body.begin(), probe.body.end(), '\n');
+    }
     int64_t nfma = 0;
-    emit_factor(f, *t, sl, P, o.tile, &nfma);
+    for (int ib = 0; ib < nb;) {
+      int end = ib + 1;
+      size_t sum = lines[ib];
+      while (end < nb && sum + lines[end] <= (size_t)o.piece_lines) sum += lines[end++];
+      pieces[m].emplace_back();
+      emit_factor(pieces[m].back(), *t, sl, P, o.tile, ib, end, &nfma);
+      ib = end;
+    }
     if (nfma != t->lu_fma) throw std::logic_error("generated factorization does not match the symbolic count");
     total += nfma;
-    fb.push_back(std::move(f.body));
-    f.body.clear();
     emit_solve(s, *t, sl, P, o.solve_block, o.solve_keep);
     sb.push_back(std::move(s.body));
     s.body.clear();
@@ -422,11 +480,7 @@ std::string generate_ptx(const std::vector<const HostTables*>& ts, const std::ve
   }
   if (fma_count) *fma_count = total;
   std::string out = ".version 9.0\n.target sm_103a\n.address_size 64\n\n";
-  out += function("fo_gen_factor",
-                  ".param .b64 fo_gen_factor_base, .param .b64 fo_gen_factor_alpha, .param .b32 fo_gen_factor_mech",
-                  f, fb,
-                  "\tld.param.b64 %p, [fo_gen_factor_base];\n\tld.param.b64 %a, [fo_gen_factor_alpha];\n"
-                  "\tld.param.b32 %m, [fo_gen_factor_mech];\n\tmov.b64 %d0, %a;\n\tcvta.to.global.u64 %b, %p;\n");
+  out += factor_functions(pieces);
   out += "\n";
   out += function("fo_gen_solve", ".param .b64 fo_gen_solve_base, .param .b32 fo_gen_solve_mech", s, sb,
                   "\tld.param.b64 %p, [fo_gen_solve_base];\n\tld.param.b32 %m, [fo_gen_solve_mech];\n"

@@ -20,6 +20,9 @@ struct GenOptions {
   int solve_block = 8;
   // values of later blocks the backward solve keeps in registers per block
   int solve_keep = 16;
+  // instructions per separately compiled piece of the factorization (whole
+  // row blocks; a block longer than this is a piece of its own)
+  int piece_lines = 40000;
 };
 
 // PTX (ISA 9.0, sm_103a) defining

@@ -85,6 +85,12 @@ const JitLink& jitlink() {
   return api;
 }
 
+// The link: sm_103a; at most 128 registers per thread, the integrator
+// kernel's budget for sixteen groups per SM, for the generated functions too;
+// ptxas optimizes the module's functions (the factorization's pieces among
+// them) on all host cores at once.
+const char* const kLinkOptions[] = {"-arch=sm_103a", "-O3", "-maxrregcount=128", "-Xptxas=--split-compile=0"};
+
 uint64_t fnv1a(uint64_t h, const void* data, size_t n) {
   const unsigned char* p = static_cast<const unsigned char*>(data);
   for (size_t i = 0; i < n; ++i) {
@@ -145,11 +151,9 @@ bool link(const std::string& ptx, std::vector<char>* cubin, std::string* err) {
     *err = api.error;
     return false;
   }
-  // the integrator kernel runs at most 128 registers per thread (sixteen
-  // groups per SM); the generated functions are compiled to the same budget
-  const char* opts[] = {"-arch=sm_103a", "-O3", "-maxrregcount=128"};
   nvJitLinkHandle h = nullptr;
-  if (api.create(&h, 3, opts) != NVJITLINK_SUCCESS) {
+  if (api.create(&h, (uint32_t)(sizeof(kLinkOptions) / sizeof(kLinkOptions[0])), kLinkOptions) !=
+      NVJITLINK_SUCCESS) {
     *err = "nvJitLinkCreate failed";
     return false;
   }
@@ -206,6 +210,7 @@ int gen_create(const std::vector<const HostTables*>& ts, const std::vector<GenOp
   h = fnv1a(h, ptx.data(), ptx.size());
   h = fnv1a(h, fo_generated_rdc_begin, (size_t)(fo_generated_rdc_end - fo_generated_rdc_begin));
   h = fnv1a(h, &runtime, sizeof(runtime));
+  for (const char* o : kLinkOptions) h = fnv1a(h, o, std::strlen(o));
   char key[32];
   std::snprintf(key, sizeof(key), "gen-%016llx.cubin", (unsigned long long)h);
   const std::string dir = cache_dir ? std::string(cache_dir) : default_cache_dir();
