@@ -310,6 +310,19 @@ def test_generated_code_links_with_the_integrator(built_library):
     assert info["ptx_bytes"] > 0 and info["cubin_bytes"] > 0 and info["tile"] == 6
 
 
+def test_generated_factorization_in_pieces_links(built_library):
+    """A mechanism whose factorization is generated as several separately
+    compiled functions (120 species / 260 reactions: 49,079 multiply-adds,
+    about 100,000 instructions, three pieces of whole row blocks) links with
+    the integrator: the pieces, the dispatching fo_gen_factor and the calls
+    between them are valid for ptxas (nvJitLink, no device needed)."""
+    from fastode_gb300 import synthetic as syn
+    sm = syn.synthetic_mechanism(120, 260, 13, third_body_fraction=0.1)
+    rc, info, err = _gen_check(sm.mech, link=True)
+    assert rc == 0, err
+    assert info["cubin_bytes"] > 0
+
+
 @pytest.mark.parametrize("case", CASES)
 def test_generated_code_covers_every_update(built_library, case):
     """Generation alone (no link) for the fixtures' mechanisms, the 210/500
